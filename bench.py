@@ -1,0 +1,429 @@
+"""Benchmark: GTEPS per label-propagation iteration on one GB300 (and N replicas).
+
+A step is one full galp run: labels reset to vertex IDs, 10 synchronous iterations of
+the exact method-0 update over the whole graph (early exit off, so every step does the
+same work).  GTEPS/iter = iterations x m / seconds, m = CSR entries (both directions).
+
+  value     device-resident: CSR already in HBM; CUDA events on the launching stream
+  e2e       through the C ABI with host buffers: galp_create (pinned H2D upload and
+            schedule) + galp_run (10 iterations + labels D2H) + galp_destroy per step
+  roofline  the dominant kernel's algorithmic bytes per launch / its event-timed duration
+  cpu_baseline  the reference's CPU label update (port of CPUWorker::update_label,
+            OpenMP over all host cores) on a bounded sample of the same graph
+
+`--impl reference` times that CPU update alone, as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (kind, params)
+    "rmat26": ("rmat", dict(scale=26, edge_factor=28)),
+    "rmat24": ("rmat", dict(scale=24, edge_factor=16)),
+    "rmat20": ("rmat", dict(scale=20, edge_factor=16)),
+    "lfr1m": ("lfr", dict(n=1_000_000)),
+    "sbm16k": ("sbm", dict()),
+}
+NITER = 10
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _rank_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+
+def rmat_on_gpu(scale: int, edge_factor: int, seed: int = 1, a=0.57, b=0.19, c=0.19):
+    """R-MAT graph built on the device: raw edges from the library's counter-based
+    sampler (same edges as the CPU generator), then symmetrise, drop self-loops and
+    duplicates, delete isolated vertices and compact IDs.  Returns device tensors
+    (offsets int64[n+1], neighbors int32[m])."""
+    import torch
+
+    import galp_gb300
+
+    L = galp_gb300.load_library()
+    L.galp_gen_rmat_keys_device.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+    L.galp_gen_rmat_keys_device.restype = ctypes.c_int
+    ne = edge_factor << scale
+    keys = torch.empty(ne, dtype=torch.int64, device="cuda")
+    rc = L.galp_gen_rmat_keys_device(seed, scale, ne, a, b, c, keys.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert rc == 0, rc
+    u = keys >> 32
+    v = keys & 0xFFFFFFFF
+    del keys
+    keep = u != v
+    u, v = u[keep], v[keep]
+    del keep
+    # bucket by the source's top bits so every sort stays below 2^31 elements
+    nb = 64 if scale >= 6 else 1
+    shift = scale - (nb.bit_length() - 1)
+    parts_src, parts_dst = [], []
+    for bkt in range(nb):
+        mu = (u >> shift) == bkt
+        mv = (v >> shift) == bkt
+        kb = torch.cat([(u[mu] << 32) | v[mu], (v[mv] << 32) | u[mv]])
+        del mu, mv
+        kb = torch.unique(kb)  # sorted, deduplicated
+        parts_src.append((kb >> 32).to(torch.int32))
+        parts_dst.append((kb & 0xFFFFFFFF).to(torch.int32))
+        del kb
+    del u, v
+    src = torch.cat(parts_src)
+    del parts_src
+    dst = torch.cat(parts_dst)
+    del parts_dst
+    deg = torch.bincount(src, minlength=1 << scale)
+    del src
+    nz = deg > 0
+    newid = (torch.cumsum(nz.to(torch.int64), 0) - 1).to(torch.int32)
+    n = int(nz.sum().item())
+    nbr = torch.empty_like(dst)
+    step = 1 << 28
+    for i in range(0, dst.numel(), step):
+        nbr[i:i + step] = newid[dst[i:i + step].long()]
+    del dst
+    offsets = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    offsets[1:] = torch.cumsum(deg[nz], 0)
+    torch.cuda.synchronize()
+    return offsets, nbr
+
+
+def build_workload(name: str):
+    """Returns (host Graph with pinned arrays when a GPU is present, description)."""
+    import galp_gb300
+
+    kind, prm = WORKLOADS[name]
+    if kind == "rmat":
+        import torch
+
+        off_d, nbr_d = rmat_on_gpu(prm["scale"], prm["edge_factor"])
+        off_h = torch.empty(off_d.numel(), dtype=torch.int64, pin_memory=True)
+        nbr_h = torch.empty(nbr_d.numel(), dtype=torch.int32, pin_memory=True)
+        off_h.copy_(off_d)
+        nbr_h.copy_(nbr_d)
+        del off_d, nbr_d
+        torch.cuda.empty_cache()
+        g = galp_gb300.Graph(off_h.numpy(), nbr_h.numpy())
+        g._pinned = (off_h, nbr_h)  # keep the pinned storage alive
+        desc = dict(workload=f"rmat-scale{prm['scale']}-ef{prm['edge_factor']}", a=0.57, b=0.19, c=0.19,
+                    seed=1, symmetrised=True, dedup=True, isolated_removed=True)
+    elif kind == "lfr":
+        g = galp_gb300.generate_lfr(prm["n"], seed=1)
+        desc = dict(workload="lfr-style-n1M", tau1=2.5, mean_deg=20, max_deg=1000, tau2=1.5, cmin=20, cmax=1000,
+                    mu=0.3, seed=1)
+    else:
+        g = galp_gb300.generate_sbm([256] * 64, 16.0, 2.0, seed=1)
+        desc = dict(workload="sbm-n16384-64x256-din16-dout2", seed=1)
+    desc.update(n=int(g.n), m=int(g.m))
+    return g, desc
+
+
+# ---------------------------------------------------------------------------
+# measurement helpers
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _loop(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._loop, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 4 + i and
+                          s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(workload)
+    return None
+
+
+def cpu_sample(g, target_s: float = 12.0, threads: int = 0):
+    """Time the reference's CPU update on a bounded prefix of the vertices sized for
+    about target_s seconds (one sweep, labels from vertex IDs)."""
+    import oracle
+
+    n, m = g.n, g.m
+    off = np.asarray(g.offsets)
+    # calibrate on ~1% of the edges (at least 2M)
+    e_cal = min(m, max(2_000_000, m // 100))
+    v_cal = int(np.searchsorted(off, e_cal))
+    v_cal = max(1, min(n, v_cal))
+    secs, used, _, _ = oracle.cpu_baseline(off, g.neighbors, 1, 0, v_cal, threads)
+    rate = (off[v_cal] - off[0]) / max(secs, 1e-6)
+    e_tgt = min(m, int(rate * target_s))
+    v_s = max(1, min(n, int(np.searchsorted(off, e_tgt))))
+    secs, used, _, _ = oracle.cpu_baseline(off, g.neighbors, 1, 0, v_s, threads)
+    edges = int(off[v_s] - off[0])
+    return dict(seconds=secs, threads=used, edges=edges, vertices=v_s)
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_reference(args, g, desc, rank, world):
+    res = None
+    for _ in range(args.warmup):
+        cpu_sample(g, target_s=args.cpu_seconds / 4)
+    vals = []
+    for _ in range(args.steps):
+        s = cpu_sample(g, target_s=args.cpu_seconds)
+        res = s
+        vals.append(s["edges"] / s["seconds"] / 1e9)
+    v = statistics.median(vals)
+    sample = (f"one sweep of CPUWorker::update_label over vertices [0, {res['vertices']}) "
+              f"({res['edges']} CSR entries of {g.m}), labels = vertex IDs")
+    line = {
+        "metric": "GTEPS per LP iteration", "value": round(v, 4), "unit": "GTEPS", "impl": "reference",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": desc,
+        "ms_per_step": round(1e3 * res["seconds"], 3),
+        "cpu_baseline": {"value": round(v, 4), "unit": "GTEPS", "cores": res["threads"], "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(v, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def run_gpu(args, g, desc, rank, world, dist):
+    import torch
+
+    import galp_gb300
+
+    L = galp_gb300.load_library()
+    from galp_gb300 import tools
+
+    dev = torch.cuda.current_device()
+    peak, peak_kind = measured_peaks()
+    stream = torch.cuda.current_stream()
+    # device-resident arm
+    p = galp_gb300.Propagator(g, early_exit=0, device=dev)
+    p.set_stream(stream.cuda_stream)
+    info = tools.schedule_info(p)
+    for _ in range(args.warmup):
+        p.enqueue(NITER)
+    p.sync()
+    tools.profile(p, True)
+    tools.profile_read(p)  # discard
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            p.enqueue(NITER)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    st = p.sync()
+    kt = tools.profile_read(p)
+    if st.err:
+        raise RuntimeError(f"device error bits {st.err}")
+    t_max = ms
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    ms_per_step = t_max / args.steps
+    edges_all = world * NITER * g.m * args.steps
+    value = edges_all / (t_max / 1e3) / 1e9
+
+    # roofline of the dominant kernel group
+    n, m, mb = info.n, info.m, info.m_big
+    # algorithmic bytes: 4 B neighbour + 4 B gathered label per CSR entry, 8 B offset,
+    # 4 B old + 4 B new label per vertex (8m + 16n + 8 per dense iteration)
+    tile_bytes = 8 * (m - mb) + 16 * n + 8
+    big_bytes = 8 * mb
+    shares = {"lp_tile_kernel": kt.tile_ms, "big_vertex_kernels": kt.big_pre_ms + kt.big_post_ms}
+    dom = max(shares, key=shares.get)
+    if dom == "lp_tile_kernel":
+        launches = max(kt.tile_launches, 1)
+        dur = kt.tile_ms / launches
+        alg = tile_bytes
+    else:
+        launches = max(kt.big_pre_groups, 1)
+        dur = (kt.big_pre_ms + kt.big_post_ms) / launches
+        alg = big_bytes
+    achieved = alg / (dur / 1e3) / 1e9
+    traffic = ncu_traffic(desc["workload"])
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                "alg_bytes_per_launch": int(alg), "avg_launch_ms": round(dur, 4),
+                "kernel_share": {k: round(v / max(sum(shares.values()), 1e-9), 3) for k, v in shares.items()}}
+    p.close()
+    del p
+
+    # end-to-end arm through the C ABI with host buffers
+    e2e_times = []
+    h2d = d2h = 0
+    for i in range(args.warmup + args.steps):
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        q = galp_gb300.Propagator(g, early_exit=0, device=dev)
+        q.run(NITER)
+        lab = q.get_labels()
+        h2d, d2h = q.stats.h2d_bytes, q.stats.d2h_bytes
+        q.close()
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_times.append(dt)
+    e2e_t = statistics.median(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_t], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_val = world * NITER * g.m / e2e_t / 1e9
+    del lab
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        s = cpu_sample(g, target_s=args.cpu_seconds)
+        cpu = {"value": round(s["edges"] / s["seconds"] / 1e9, 4), "unit": "GTEPS", "cores": s["threads"],
+               "kind": "port",
+               "sample": (f"one sweep of CPUWorker::update_label (port) over vertices [0, {s['vertices']}) = "
+                          f"{s['edges']} of {g.m} CSR entries, OpenMP dynamic schedule")}
+    launches_step = 2 + 2 + NITER * info.launches_per_iter  # init labels/ctl + per-iteration kernels
+    cfg = dict(desc)
+    cfg.update(iterations_per_step=NITER, early_exit=False, method=0, policy=0,
+               l2="inputs larger than L2 (neighbours {:.1f} GB vs 129 MB L2)".format(4 * g.m / 1e9),
+               parallelism="replicas" if world > 1 else "single-gpu", ntiles=int(info.ntiles),
+               big_vertices=int(info.nbig), big_edges=int(info.m_big))
+    line = {
+        "metric": "GTEPS per LP iteration", "value": round(value, 3), "unit": "GTEPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic", "config": cfg, "clocks": clk.summary(), "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_val, 3), "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_t, 4)},
+        "gpu_launches": int(launches_step * args.steps),
+        "iteration_ms": round(ms_per_step / NITER, 4),
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="galp", choices=["galp", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("GALP_BENCH_WORKLOAD", "rmat26"), choices=list(WORKLOADS))
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = _rank_env()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from galp_gb300.build import build
+
+        build()
+        import torch
+
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        g, desc = build_workload(args.workload)
+        print(json.dumps(run_reference(args, g, desc, rank, world)))
+        return 0
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+        dist = tdist
+    torch.cuda.set_device(local)
+    from galp_gb300.build import build
+
+    if rank == 0:
+        build()
+    if dist:
+        dist.barrier()
+    g, desc = build_workload(args.workload)
+    line = run_gpu(args, g, desc, rank, world, dist)
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

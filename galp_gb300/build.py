@@ -1,0 +1,116 @@
+"""Build the native parts of galp-gb300 in-tree.
+
+Products (all under galp_gb300/lib/ unless noted):
+  libgalp.so       CUDA label-propagation library behind include/galp.h (sm_103a)
+  libgalp_gen.so   seeded graph generators behind include/galp_gen.h
+  libgalp_host.so  front end: .txt/.bin loaders and accuracy measures (include/galp_host.h)
+  galp             the command-line front end (src mirrors the reference's main.cu CLI)
+and the test-infrastructure oracle:
+  oracle/_build/liblp_oracle.so   CPU restatement of the reference update
+  oracle/_ref/ref_harness         reference kernels run on the CPU (only where the
+                                  reference tree is present)
+
+Every step is a direct nvcc/g++ invocation; the steps run in parallel.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "galp_gb300")
+CSRC = os.path.join(PKG, "csrc")
+LIB = os.path.join(PKG, "lib")
+ORACLE = os.path.join(ROOT, "oracle")
+
+NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+CUDA_SOURCES = ["galp_capi.cu", "galp_tools.cu"]
+HOST_SOURCES = ["host/graph_io.cpp", "host/accuracy.cpp"]
+
+
+def _run(cmd: list[str]) -> tuple[list[str], int, str]:
+    p = subprocess.run(cmd, cwd=ROOT, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    return cmd, p.returncode, p.stdout
+
+
+def _newer(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return False
+    t = os.path.getmtime(target)
+    return all(os.path.getmtime(d) <= t for d in deps if os.path.exists(d))
+
+
+def _deps(*dirs: str) -> list[str]:
+    out = []
+    for d in dirs:
+        for base, _, files in os.walk(d):
+            if "_ref" in base or "_build" in base or "lib" == os.path.basename(base):
+                continue
+            out += [os.path.join(base, f) for f in files if f.endswith((".cu", ".cuh", ".h", ".cpp", ".c"))]
+    return out
+
+
+def build(force: bool = False, verbose: bool = False) -> None:
+    os.makedirs(LIB, exist_ok=True)
+    os.makedirs(os.path.join(ORACLE, "_build"), exist_ok=True)
+    inc = os.path.join(ROOT, "include")
+    jobs: list[tuple[str, list[str], list[str]]] = []
+
+    cuda_out = os.path.join(LIB, "libgalp.so")
+    cuda_deps = _deps(CSRC, inc)
+    jobs.append((cuda_out, cuda_deps, [NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                                       "-shared", "-o", cuda_out,
+                                       *[os.path.join(CSRC, s) for s in CUDA_SOURCES]]))
+
+    gen_out = os.path.join(LIB, "libgalp_gen.so")
+    gen_src = os.path.join(PKG, "gen", "generators.cpp")
+    jobs.append((gen_out, [gen_src, os.path.join(inc, "galp_gen.h")],
+                 ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-o", gen_out, gen_src]))
+
+    host_srcs = [os.path.join(PKG, s) for s in HOST_SOURCES]
+    host_out = os.path.join(LIB, "libgalp_host.so")
+    if all(os.path.exists(s) for s in host_srcs):
+        jobs.append((host_out, host_srcs + [os.path.join(inc, "galp_host.h")],
+                     ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-o", host_out, *host_srcs]))
+        cli_src = os.path.join(PKG, "host", "main.cpp")
+        cli_out = os.path.join(LIB, "galp")
+        if os.path.exists(cli_src):
+            jobs.append((cli_out, [cli_src, *host_srcs, os.path.join(inc, "galp.h")],
+                         [NVCC, *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fopenmp", "-o", cli_out, cli_src,
+                          *host_srcs, *[os.path.join(CSRC, s) for s in CUDA_SOURCES], "-lgomp"]))
+
+    orc_out = os.path.join(ORACLE, "_build", "liblp_oracle.so")
+    orc_src = [os.path.join(ORACLE, "lp_oracle.c")]
+    jobs.append((orc_out, orc_src, ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-o", orc_out, *orc_src]))
+    port_src = os.path.join(ORACLE, "cpu_worker_port.cpp")
+    if os.path.exists(port_src):
+        port_out = os.path.join(ORACLE, "_build", "libcpu_worker_port.so")
+        jobs.append((port_out, [port_src], ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-o",
+                                            port_out, port_src]))
+
+    todo = [(o, cmd) for o, deps, cmd in jobs if force or not _newer(o, deps)]
+    ref_script = os.path.join(ORACLE, "build_ref.sh")
+    ref_needed = os.path.isdir(os.environ.get("GALP_REFERENCE", "/root/reference")) and (
+        force or not _newer(os.path.join(ORACLE, "_ref", "ref_harness"), _deps(os.path.join(ORACLE, "refsim"))))
+    with ThreadPoolExecutor(max_workers=max(1, len(todo) + 1)) as ex:
+        futs = [ex.submit(_run, cmd) for _, cmd in todo]
+        if ref_needed:
+            futs.append(ex.submit(_run, ["bash", ref_script]))
+        failed = []
+        for f in futs:
+            cmd, rc, out = f.result()
+            if verbose or rc:
+                sys.stderr.write(" ".join(cmd) + "\n" + out)
+            if rc:
+                failed.append(cmd[-1])
+    if failed:
+        raise RuntimeError("galp_gb300 build failed: " + ", ".join(failed))
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose="-v" in sys.argv)

@@ -1,0 +1,555 @@
+// galp_capi.cu -- host side of the C ABI (include/galp.h): context, schedule, launches.
+//
+// In-core (policy 0) keeps the whole CSR resident in HBM: neighbours int32[m],
+// offsets int64[n+1] (no int32 truncation, unlike src/common/incore.cuh:63-69),
+// two label buffers, and a static schedule built once per graph:
+//   vpos[n]      uint16 slot of each vertex inside its tile
+//   tile_v0[T+1] first vertex of each tile, tile_used[T] slots used,
+//   tile_big[T]  big-vertex index for single-vertex tiles of degree > kTileSlots
+// plus open-addressed global tables for the big vertices.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <vector>
+
+#include "../../include/galp.h"
+#include "lp_kernels.cuh"
+#include "galp_ctx.h"
+#include "../../include/galp_tools.h"
+
+using namespace galp;
+
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+namespace galp {
+
+int cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return GALP_OK;
+    if (e == cudaErrorMemoryAllocation) return GALP_ENOMEM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GALP_ENODEV;
+    return GALP_ECUDA;
+}
+
+#define GALP_CUDA(call)                                    \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_status(e_);     \
+    } while (0)
+
+// Static per-graph schedule (host): tiles of consecutive vertices whose labels fit
+// kTileSlots shared-memory slots, small vertices (degree <= 32) never straddling a
+// 32-slot pack, larger ones starting on a pack boundary; vertices above
+// kTileSlots become single-vertex big tiles.
+void build_schedule(Schedule &S, int64_t n, const int64_t *off)
+{
+    S.vpos.assign((size_t)n, 0);
+    S.tile_v0.clear();
+    S.tile_big.clear();
+    S.tile_used.clear();
+    S.big_v.clear();
+    S.last_v = -1;
+    int cur = 0, nvt = 0;
+    int64_t tstart = 0;
+    auto close = [&](int64_t vend) {
+        if (vend > tstart) {
+            S.tile_v0.push_back((int32_t)tstart);
+            S.tile_big.push_back(-1);
+            S.tile_used.push_back((uint16_t)cur);
+        }
+        tstart = vend;
+        cur = 0;
+        nvt = 0;
+    };
+    for (int64_t v = 0; v < n; ++v) {
+        const int64_t deg = off[v + 1] - off[v];
+        if (deg > 0) S.last_v = (int32_t)v;
+        if (deg > kTileSlots) {
+            close(v);
+            S.tile_v0.push_back((int32_t)v);
+            S.tile_big.push_back((int32_t)S.big_v.size());
+            S.tile_used.push_back(0);
+            S.big_v.push_back((int32_t)v);
+            tstart = v + 1;
+            continue;
+        }
+        auto place = [&](int c, int &pos, int &end) {
+            if (deg == 0) {
+                pos = c;
+                end = c;
+            } else if (deg <= kSmallMax) {
+                pos = ((c & 31) + (int)deg > 32) ? ((c + 31) & ~31) : c;
+                end = pos + (int)deg;
+            } else {
+                pos = (c + 31) & ~31;
+                end = pos + (((int)deg + 31) & ~31);
+            }
+        };
+        int pos, end;
+        place(cur, pos, end);
+        if (nvt == kTileV || end > kTileSlots) {
+            close(v);
+            place(0, pos, end);
+        }
+        S.vpos[v] = (uint16_t)pos;
+        cur = end;
+        nvt++;
+    }
+    close(n);
+    S.tile_v0.push_back((int32_t)n);
+
+    // big-vertex tables and work lists
+    S.big_toff.clear();
+    S.big_tcap.clear();
+    S.chunk_big.clear();
+    S.chunk_e0.clear();
+    S.chunk_e1.clear();
+    S.schunk_big.clear();
+    S.schunk_s0.clear();
+    S.schunk_s1.clear();
+    int64_t toff = 0;
+    for (size_t b = 0; b < S.big_v.size(); ++b) {
+        const int64_t v = S.big_v[b];
+        const int64_t deg = off[v + 1] - off[v];
+        uint32_t cap = 1;
+        while ((int64_t)cap < 2 * deg) cap <<= 1;
+        S.big_toff.push_back(toff);
+        S.big_tcap.push_back(cap);
+        for (int64_t e = off[v]; e < off[v + 1]; e += kBigChunk) {
+            S.chunk_big.push_back((int32_t)b);
+            S.chunk_e0.push_back(e);
+            S.chunk_e1.push_back(std::min<int64_t>(e + kBigChunk, off[v + 1]));
+        }
+        for (int64_t s = 0; s < cap; s += kBigSlotChunk) {
+            S.schunk_big.push_back((int32_t)b);
+            S.schunk_s0.push_back(toff + s);
+            S.schunk_s1.push_back(toff + std::min<int64_t>(s + kBigSlotChunk, cap));
+        }
+        toff += cap;
+    }
+    S.table_slots = toff;
+}
+
+int64_t big_edges(const Schedule &S, const int64_t *off)
+{
+    int64_t mb = 0;
+    for (int32_t v : S.big_v) mb += off[v + 1] - off[v];
+    return mb;
+}
+
+template <class T>
+int upload(DevBuf &owner, T *&dst, const std::vector<T> &src, cudaStream_t st, int64_t &h2d)
+{
+    const size_t bytes = sizeof(T) * std::max<size_t>(src.size(), 1);
+    GALP_CUDA(owner.alloc(bytes));
+    dst = (T *)owner.p;
+    if (!src.empty()) {
+        GALP_CUDA(cudaMemcpyAsync(dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, st));
+        h2d += (int64_t)(sizeof(T) * src.size());
+    }
+    return GALP_OK;
+}
+
+int InCore::setup(const galp_csr &g, cudaStream_t st, int64_t &h2d)
+{
+    n = g.n;
+    m = g.m;
+    build_schedule(sched, n, g.offsets);
+    m_big = big_edges(sched, g.offsets);
+    GALP_CUDA(b_nbr.alloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
+    GALP_CUDA(b_off.alloc(sizeof(int64_t) * (n + 1)));
+    if (m) GALP_CUDA(cudaMemcpyAsync(b_nbr.p, g.neighbors, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
+    GALP_CUDA(cudaMemcpyAsync(b_off.p, g.offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
+    h2d += sizeof(int32_t) * m + sizeof(int64_t) * (n + 1);
+    int rc;
+    if ((rc = upload(b_vpos, d_vpos, sched.vpos, st, h2d))) return rc;
+    if ((rc = upload(b_tile_v0, d_tile_v0, sched.tile_v0, st, h2d))) return rc;
+    if ((rc = upload(b_tile_big, d_tile_big, sched.tile_big, st, h2d))) return rc;
+    if ((rc = upload(b_tile_used, d_tile_used, sched.tile_used, st, h2d))) return rc;
+    if ((rc = upload(b_big_v, d_big_v, sched.big_v, st, h2d))) return rc;
+    if ((rc = upload(b_big_toff, d_big_toff, sched.big_toff, st, h2d))) return rc;
+    if ((rc = upload(b_big_tcap, d_big_tcap, sched.big_tcap, st, h2d))) return rc;
+    if ((rc = upload(b_chunk_big, d_chunk_big, sched.chunk_big, st, h2d))) return rc;
+    if ((rc = upload(b_chunk_e0, d_chunk_e0, sched.chunk_e0, st, h2d))) return rc;
+    if ((rc = upload(b_chunk_e1, d_chunk_e1, sched.chunk_e1, st, h2d))) return rc;
+    if ((rc = upload(b_schunk_big, d_schunk_big, sched.schunk_big, st, h2d))) return rc;
+    if ((rc = upload(b_schunk_s0, d_schunk_s0, sched.schunk_s0, st, h2d))) return rc;
+    if ((rc = upload(b_schunk_s1, d_schunk_s1, sched.schunk_s1, st, h2d))) return rc;
+    GALP_CUDA(b_lab0.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
+    GALP_CUDA(b_lab1.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
+    const size_t ntiles = sched.tile_big.size();
+    GALP_CUDA(b_status.alloc(sizeof(unsigned long long) * std::max<size_t>(ntiles, 1)));
+    GALP_CUDA(cudaMemsetAsync(b_status.p, 0, sizeof(unsigned long long) * std::max<size_t>(ntiles, 1), st));
+    GALP_CUDA(b_ctl.alloc(sizeof(Ctl)));
+    const size_t nbig = sched.big_v.size();
+    GALP_CUDA(b_bstat.alloc(sizeof(BigStat) * std::max<size_t>(nbig, 1)));
+    GALP_CUDA(b_big_a.alloc(sizeof(int64_t) * std::max<size_t>(nbig, 1)));
+    GALP_CUDA(b_gkey.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.table_slots, 1)));
+    GALP_CUDA(b_gcnt.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.table_slots, 1)));
+    if (sched.table_slots) {
+        GALP_CUDA(cudaMemsetAsync(b_gkey.p, 0xFF, sizeof(uint32_t) * sched.table_slots, st));
+        GALP_CUDA(cudaMemsetAsync(b_gcnt.p, 0, sizeof(uint32_t) * sched.table_slots, st));
+    }
+    if (nbig) {
+        init_bigstat_kernel<<<(unsigned)((nbig + 255) / 256), 256, 0, st>>>((BigStat *)b_bstat.p, (int)nbig);
+        GALP_CUDA(cudaGetLastError());
+    }
+    // validate the graph on the device before any iteration touches it
+    GALP_CUDA(b_bad.alloc(sizeof(int)));
+    GALP_CUDA(cudaMemsetAsync(b_bad.p, 0, sizeof(int), st));
+    validate_kernel<<<1024, 256, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr.p, n, m, (int *)b_bad.p);
+    GALP_CUDA(cudaGetLastError());
+    int bad = 0;
+    GALP_CUDA(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GALP_CUDA(cudaStreamSynchronize(st));
+    if (bad) return GALP_EFORMAT;
+
+    int dev = 0, sms = 0;
+    GALP_CUDA(cudaGetDevice(&dev));
+    GALP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GALP_CUDA(cudaFuncSetAttribute(lp_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)));
+    int occ = 0;
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lp_tile_kernel, kTB, sizeof(TileSmem)));
+    tile_grid = (int)std::min<int64_t>((int64_t)std::max(occ, 1) * sms, std::max<size_t>(ntiles, 1));
+    return GALP_OK;
+}
+
+IterArgs InCore::args() const
+{
+    IterArgs a{};
+    a.nbr = (const int32_t *)b_nbr.p;
+    a.off = (const int64_t *)b_off.p;
+    a.vpos = d_vpos;
+    a.tile_v0 = d_tile_v0;
+    a.tile_big = d_tile_big;
+    a.tile_used = d_tile_used;
+    a.ntiles = (int32_t)sched.tile_big.size();
+    a.last_v = sched.last_v;
+    a.status = (unsigned long long *)b_status.p;
+    a.ctl = (Ctl *)b_ctl.p;
+    a.nbig = (int32_t)sched.big_v.size();
+    a.big_v = d_big_v;
+    a.big_toff = d_big_toff;
+    a.big_tcap = d_big_tcap;
+    a.chunk_big = d_chunk_big;
+    a.chunk_e0 = d_chunk_e0;
+    a.chunk_e1 = d_chunk_e1;
+    a.nchunks = (int32_t)sched.chunk_big.size();
+    a.schunk_big = d_schunk_big;
+    a.schunk_s0 = d_schunk_s0;
+    a.schunk_s1 = d_schunk_s1;
+    a.nschunks = (int32_t)sched.schunk_big.size();
+    a.gkey = (uint32_t *)b_gkey.p;
+    a.gcnt = (uint32_t *)b_gcnt.p;
+    a.bstat = (BigStat *)b_bstat.p;
+    a.big_a = (int64_t *)b_big_a.p;
+    return a;
+}
+
+// one iteration reading lab_in, writing lab_out
+int InCore::enqueue_iteration(cudaStream_t st, const int32_t *lab_in, int32_t *lab_out)
+{
+    IterArgs a = args();
+    a.lab_in = lab_in;
+    a.lab_out = lab_out;
+    if (++epoch > (unsigned)kEpochMask) {
+        epoch = 1;
+        GALP_CUDA(cudaMemsetAsync(b_status.p, 0, sizeof(unsigned long long) * std::max<int32_t>(a.ntiles, 1), st));
+    }
+    a.epoch = epoch;
+    int e0 = -1;
+    if (a.nbig) {
+        if (prof.on) e0 = prof.mark(st);
+        big_insert_kernel<<<a.nchunks, kTB, 0, st>>>(a);
+        for (int pass = 0; pass < 3; ++pass) big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a, pass);
+        if (prof.on) prof.spans[1].push_back({e0, prof.mark(st)});
+    }
+    if (prof.on) e0 = prof.mark(st);
+    lp_tile_kernel<<<tile_grid, kTB, sizeof(TileSmem), st>>>(a);
+    if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
+    if (a.nbig) {
+        if (prof.on) e0 = prof.mark(st);
+        big_resolve_kernel<<<a.nbig, 32, sizeof(uint32_t) * kPickScratch, st>>>(a);
+        big_clear_kernel<<<1024, 256, 0, st>>>(a.gkey, a.gcnt, sched.table_slots, a.ctl);
+        if (prof.on) prof.spans[2].push_back({e0, prof.mark(st)});
+    }
+    finalize_kernel<<<1, 1, 0, st>>>(a.ctl);
+    GALP_CUDA(cudaGetLastError());
+    return GALP_OK;
+}
+
+int InCore::enqueue_run(cudaStream_t st, int niter, long long thr)
+{
+    int32_t *lab[2] = {(int32_t *)b_lab0.p, (int32_t *)b_lab1.p};
+    if (n > 0) {
+        const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
+        init_labels_kernel<<<blocks, 256, 0, st>>>(lab[0], n);
+    }
+    init_ctl_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p, thr, niter);
+    GALP_CUDA(cudaGetLastError());
+    for (int it = 0; it < niter; ++it) {
+        int rc = enqueue_iteration(st, lab[it & 1], lab[(it + 1) & 1]);
+        if (rc) return rc;
+    }
+    return GALP_OK;
+}
+
+}  // namespace galp
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void galp_default_opts(galp_opts *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->method = 0;
+    o->policy = 0;
+    o->lfht_policy = 1;
+    o->buffer_pow = 24;
+    o->frontier = 0;
+    o->dispatch = 0;
+    o->device = 0;
+    o->early_exit = 1;
+}
+
+const char *galp_strerror(int code)
+{
+    switch (code) {
+    case GALP_OK: return "ok";
+    case GALP_EINVAL: return "invalid argument";
+    case GALP_ENOMEM: return "out of memory";
+    case GALP_ECUDA: return "CUDA error";
+    case GALP_ETIMEOUT: return "device wait timed out";
+    case GALP_EFORMAT: return "malformed graph";
+    case GALP_EUNSUPPORTED: return "unsupported method/policy";
+    case GALP_ENODEV: return "no CUDA device";
+    case GALP_EBATCH: return "vertex degree exceeds the out-of-core batch buffer";
+    default: return "unknown error";
+    }
+}
+
+int galp_create(const galp_csr *g, const galp_opts *o, galp_ctx **out)
+{
+    if (!g || !out) return GALP_EINVAL;
+    *out = nullptr;
+    galp_opts opts;
+    if (o) opts = *o; else galp_default_opts(&opts);
+    if (g->n < 0 || g->m < 0 || g->n >= ((int64_t)1 << 31) || !g->offsets || (g->m > 0 && !g->neighbors))
+        return GALP_EINVAL;
+    if (g->offsets[0] != 0 || g->offsets[g->n] != g->m) return GALP_EFORMAT;
+    if (opts.method < 0 || opts.method > 1) return GALP_EUNSUPPORTED;
+    if (opts.policy != 0) return GALP_EUNSUPPORTED;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GALP_ENODEV;
+    if (opts.device < 0 || opts.device >= ndev) return GALP_EINVAL;
+    if (cudaSetDevice(opts.device) != cudaSuccess) return GALP_ECUDA;
+
+    std::unique_ptr<galp_ctx> ctx(new (std::nothrow) galp_ctx());
+    if (!ctx) return GALP_ENOMEM;
+    ctx->opts = opts;
+    ctx->n = g->n;
+    ctx->m = g->m;
+    const double t0 = now_s();
+    GALP_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+    ctx->stream = ctx->own_stream;
+    int rc = ctx->incore.setup(*g, ctx->stream, ctx->h2d_setup);
+    if (rc) return rc;
+    GALP_CUDA(cudaEventCreate(&ctx->ev0));
+    GALP_CUDA(cudaEventCreate(&ctx->ev1));
+    ctx->t_pre = now_s() - t0;
+    *out = ctx.release();
+    return GALP_OK;
+}
+
+int galp_set_stream(galp_ctx *ctx, void *stream)
+{
+    if (!ctx) return GALP_EINVAL;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return GALP_OK;
+}
+
+static long long exit_threshold(const galp_ctx *ctx)
+{
+    if (!ctx->opts.early_exit) return -1;  // changes are never negative: never stop early
+    return (long long)std::floor((double)ctx->n * 1e-5);
+}
+
+int galp_enqueue(galp_ctx *ctx, int32_t niter)
+{
+    if (!ctx || niter < 0) return GALP_EINVAL;
+    GALP_CUDA(cudaSetDevice(ctx->opts.device));
+    GALP_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    int rc = ctx->incore.enqueue_run(ctx->stream, niter, exit_threshold(ctx));
+    if (rc) return rc;
+    GALP_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->pending = true;
+    return GALP_OK;
+}
+
+int galp_sync(galp_ctx *ctx, galp_stats *st)
+{
+    if (!ctx) return GALP_EINVAL;
+    GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+    Ctl c;
+    GALP_CUDA(cudaMemcpy(&c, ctx->incore.b_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    ctx->iters = c.iter;
+    ctx->err = c.err;
+    ctx->runs_last = c.N;
+    for (int i = 0; i < GALP_MAX_ITERS; ++i) ctx->counts[i] = (int64_t)c.counts[i];
+    float ms = 0.f;
+    if (ctx->pending) cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ctx->pending = false;
+    ctx->device_ms = ms;
+    if (st) {
+        std::memset(st, 0, sizeof(*st));
+        st->device_ms = ms;
+        st->iters_run = c.iter;
+        st->err = c.err;
+        st->runs_last = c.N;
+        for (int i = 0; i < GALP_MAX_ITERS; ++i) st->updates[i] = (int64_t)c.counts[i];
+    }
+    return (c.err & kErrLookback) ? GALP_ETIMEOUT : GALP_OK;
+}
+
+int galp_run(galp_ctx *ctx, int32_t niter, galp_stats *st)
+{
+    if (!ctx || niter < 0) return GALP_EINVAL;
+    const double t0 = now_s();
+    int rc = galp_enqueue(ctx, niter);
+    if (rc) return rc;
+    galp_stats tmp;
+    rc = galp_sync(ctx, &tmp);
+    if (rc && rc != GALP_ETIMEOUT) return rc;
+    // final labels to the host (dpp.cuh:93)
+    ctx->labels.resize((size_t)ctx->n);
+    const int32_t *src = (ctx->iters & 1) ? (const int32_t *)ctx->incore.b_lab1.p : (const int32_t *)ctx->incore.b_lab0.p;
+    if (ctx->n) GALP_CUDA(cudaMemcpy(ctx->labels.data(), src, sizeof(int32_t) * ctx->n, cudaMemcpyDeviceToHost));
+    ctx->have_labels = true;
+    const double f1 = now_s() - t0;
+    if (st) {
+        *st = tmp;
+        st->f1 = f1;
+        st->f2 = f1 + ctx->t_pre;
+        st->h2d_bytes = ctx->h2d_setup;
+        st->d2h_bytes = (int64_t)sizeof(int32_t) * ctx->n;
+    }
+    return rc;
+}
+
+int galp_get_labels(galp_ctx *ctx, int32_t *out, int64_t n)
+{
+    if (!ctx || n != ctx->n || (!out && n > 0)) return GALP_EINVAL;
+    if (!ctx->have_labels) {
+        // labels of the last enqueued run, if any, else the initial labels
+        const int32_t *src = (ctx->iters & 1) ? (const int32_t *)ctx->incore.b_lab1.p : (const int32_t *)ctx->incore.b_lab0.p;
+        GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (n) GALP_CUDA(cudaMemcpy(out, src, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        return GALP_OK;
+    }
+    if (n) std::memcpy(out, ctx->labels.data(), sizeof(int32_t) * n);
+    return GALP_OK;
+}
+
+void galp_destroy(galp_ctx *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->opts.device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
+{
+    if (!ctx || !info) return GALP_EINVAL;
+    std::memset(info, 0, sizeof(*info));
+    const galp::InCore &ic = ctx->incore;
+    info->n = ctx->n;
+    info->m = ctx->m;
+    info->m_big = ic.m_big;
+    info->ntiles = (int64_t)ic.sched.tile_big.size();
+    info->nbig = (int64_t)ic.sched.big_v.size();
+    info->table_slots = ic.sched.table_slots;
+    info->launches_per_iter = 2 + (info->nbig ? 6 : 0);
+    return GALP_OK;
+}
+
+int galp_profile(galp_ctx *ctx, int32_t enable)
+{
+    if (!ctx) return GALP_EINVAL;
+    ctx->incore.prof.on = enable != 0;
+    return GALP_OK;
+}
+
+int galp_profile_read(galp_ctx *ctx, galp_kernel_times *out)
+{
+    if (!ctx || !out) return GALP_EINVAL;
+    std::memset(out, 0, sizeof(*out));
+    GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+    galp::Profiler &P = ctx->incore.prof;
+    double *ms[3] = {&out->tile_ms, &out->big_pre_ms, &out->big_post_ms};
+    int32_t *cnt[3] = {&out->tile_launches, &out->big_pre_groups, &out->big_post_groups};
+    for (int g = 0; g < 3; ++g) {
+        for (auto &sp : P.spans[g]) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, P.pool[sp.first], P.pool[sp.second]) == cudaSuccess) *ms[g] += t;
+            ++*cnt[g];
+        }
+        P.spans[g].clear();
+    }
+    P.used = 0;
+    return GALP_OK;
+}
+
+int32_t galp_debug_resolve_rank(int64_t a, int64_t d, int64_t N, int32_t is_last, const int32_t *cand, int32_t k)
+{
+    struct Q {
+        const int32_t *c;
+        int32_t k;
+        __host__ __device__ int first_ge(int64_t x)
+        {
+            for (int i = 0; i < k; ++i)
+                if (c[i] >= x) return c[i];
+            return -1;
+        }
+        __host__ __device__ int last_lt(int64_t y)
+        {
+            int r = -1;
+            for (int i = 0; i < k; ++i)
+                if (c[i] < y) r = c[i];
+            return r;
+        }
+        __host__ __device__ int tile_pick(int64_t lo)
+        {
+            int r = -1, best = -1;
+            for (int i = 0; i < k; ++i)
+                if (c[i] >= lo && c[i] < lo + galp::kTile && galp::tile_priority(c[i] - lo) > best) {
+                    best = galp::tile_priority(c[i] - lo);
+                    r = c[i];
+                }
+            return r;
+        }
+    } q{cand, k};
+    if (!cand || k <= 0 || d <= 0) return -1;
+    return galp::resolve_rank(a, d, N, is_last != 0, q);
+}
+
+}  // extern "C"

@@ -1,0 +1,65 @@
+// lp_device.cuh -- device-side building blocks of the exact label-propagation update.
+//
+// Semantics reproduced (reference: label_propagation/src/dpp/dpp.cuh:104-138 and
+// src/common/segmented_reduce.cuh:26-626): vertex v's neighbour labels, sorted
+// ascending and run-length encoded, form runs [a, a+d) of a scope-wide run array
+// (a = sum of the distinct-label counts of all earlier vertices in the scope).
+// The new label is the label of the heaviest run, ties broken by the run's
+// global position through the reference's segmented arg-max, whose closed form
+// is resolve_rank() below.  Only the positions of the maximum-count runs
+// ("candidates") matter: a lighter run never wins a comparison, and between
+// candidates every comparison is decided by position alone.
+#pragma once
+
+#include <cstdint>
+#include <climits>
+
+#include "lp_resolve.h"
+
+namespace galp {
+
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;  // hash-table empty key (labels are < 2^31)
+
+__device__ __forceinline__ uint32_t mix32(uint32_t x)
+{
+    // murmur3 finaliser
+    x ^= x >> 16;
+    x *= 0x85EBCA6Bu;
+    x ^= x >> 13;
+    x *= 0xC2B2AE35u;
+    x ^= x >> 16;
+    return x;
+}
+
+// slot in [0, cap) for key x
+__device__ __forceinline__ uint32_t hslot(uint32_t x, uint32_t cap)
+{
+    return __umulhi(mix32(x), cap);
+}
+
+// ----- relaxed 64-bit global accesses for the look-back status words -----
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v)
+{
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Status word of one tile in the decoupled look-back scan:
+//   [63:62] state (1 = aggregate, 2 = inclusive prefix), [61:40] epoch, [39:0] value
+constexpr int kStateShift = 62;
+constexpr int kEpochShift = 40;
+constexpr unsigned long long kValueMask = (1ull << 40) - 1;
+constexpr unsigned long long kEpochMask = (1ull << 22) - 1;
+
+__device__ __forceinline__ unsigned long long pack_status(unsigned state, unsigned epoch, unsigned long long value)
+{
+    return ((unsigned long long)state << kStateShift) | ((unsigned long long)(epoch & kEpochMask) << kEpochShift) |
+           (value & kValueMask);
+}
+
+}  // namespace galp

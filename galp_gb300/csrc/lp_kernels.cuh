@@ -1,0 +1,973 @@
+// lp_kernels.cuh -- kernels of one exact label-propagation iteration (method-0 semantics).
+//
+// One iteration over a scope (whole graph in-core, one batch out-of-core, one graph
+// of a batch) is:
+//
+//   big_insert  -> big_stats x3 -> lp_tile_kernel -> big_resolve -> big_clear -> finalize
+//
+// lp_tile_kernel is a persistent, single-pass kernel: CTAs take vertex tiles in
+// vertex order from an atomic ticket, gather the tile's neighbour labels into shared
+// memory once, count them (warp match for vertices of degree <= 32, a per-vertex
+// shared-memory hash region for larger ones), publish the tile's distinct-label
+// total, obtain the exclusive prefix (the run base of the tile's first vertex) by
+// decoupled look-back over the preceding tiles, and resolve every vertex's winner
+// with the positional tie rule while the tile is still on chip.  Vertices of degree
+// above kTileSlots ("big") are counted beforehand into global hash tables by
+// big_insert/big_stats, take part in the scan as single-vertex tiles, and are
+// resolved by big_resolve once their run base is known.
+//
+// Reference counterparts: DPPBase::perform_lp (label_propagation/src/dpp/dpp.cuh:104-138),
+// gather_labels..update_labels (src/dpp/kernel.cuh:27-119), the segmented sort and
+// scan (dpp.cuh:113-118) and SegmentedReducer::apply (src/common/segmented_reduce.cuh:586-615).
+#pragma once
+
+#include <cstdint>
+#include <climits>
+
+#include "lp_device.cuh"
+
+namespace galp {
+
+constexpr int kTB = 256;              // threads per CTA
+constexpr int kNW = kTB / 32;         // warps per CTA
+constexpr int kTileSlots = 2048;      // shared-memory label slots per tile
+constexpr int kTileV = 512;           // vertices per tile
+constexpr int kSmallMax = 32;         // degree handled by one warp pack
+constexpr int kBigChunk = 4096;       // edges per big_insert CTA
+constexpr int kBigSlotChunk = 8192;   // table slots per big_stats CTA
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
+constexpr long long kSpinLimit = 1ll << 20;  // look-back give-up bound (about a second)
+
+// error bits in Ctl::err
+constexpr int kErrLookback = 1;
+
+struct Ctl {
+    int active;                 // 1 while iterations still run
+    int iter;                   // iterations completed
+    int err;                    // sticky error bits
+    int pad0;
+    unsigned long long ticket;  // tile ticket of the running lp_tile_kernel
+    unsigned long long changes; // labels changed in the current iteration
+    long long N;                // runs in the scope (written by the tile of last_v)
+    long long thr;              // early-exit threshold: stop when changes <= thr
+    int max_iter;               // iterations requested
+    int pad1;
+    unsigned long long counts[64];  // changes per iteration
+};
+
+// Per-big-vertex statistics (reset by big_resolve after use).
+struct BigStat {
+    int d;      // distinct labels
+    int W;      // max count
+    int k;      // candidates
+    int cmin;   // smallest candidate label
+    int cmax;   // largest candidate label
+    int rmin;   // rank of cmin
+    int rmax;   // rank of cmax
+    int pad;
+};
+
+struct IterArgs {
+    const int32_t *nbr;        // CSR neighbours (global IDs)
+    const int64_t *off;        // CSR offsets (global)
+    const uint16_t *vpos;      // slot position of each vertex in its tile
+    const int32_t *tile_v0;    // ntiles+1: first vertex of each tile
+    const int32_t *tile_big;   // ntiles: big-vertex index or -1
+    const uint16_t *tile_used; // ntiles: slots used by the tile
+    int32_t ntiles;
+    int32_t last_v;            // last vertex that owns runs, or -1
+    const int32_t *lab_in;
+    int32_t *lab_out;
+    unsigned long long *status;
+    unsigned epoch;
+    Ctl *ctl;
+    // big vertices
+    int32_t nbig;
+    const int32_t *big_v;       // vertex of each big entry
+    const int64_t *big_toff;    // table offset of each big entry
+    const uint32_t *big_tcap;   // table capacity (power of two)
+    const int32_t *chunk_big;   // insert chunk -> big index
+    const int64_t *chunk_e0;    // insert chunk -> first edge
+    const int64_t *chunk_e1;    // insert chunk -> end edge
+    int32_t nchunks;
+    const int32_t *schunk_big;  // stats chunk -> big index
+    const int64_t *schunk_s0;   // stats chunk -> first table slot (global)
+    const int64_t *schunk_s1;
+    int32_t nschunks;
+    uint32_t *gkey;             // big tables: keys
+    uint32_t *gcnt;             // big tables: counts
+    BigStat *bstat;
+    int64_t *big_a;             // run base of each big vertex (written by the scan)
+};
+
+__device__ __forceinline__ int pad32(int x) { return (x + 31) & ~31; }
+
+__device__ __forceinline__ bool ctl_active(const Ctl *c)
+{
+    return *((volatile const int *)&c->active) != 0;
+}
+
+// ---------------------------------------------------------------------------
+// warp helpers
+// ---------------------------------------------------------------------------
+
+// max over the contiguous lane segment [first, last] containing this lane
+__device__ __forceinline__ int seg_max(int val, int lane, int first, int last)
+{
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int o = __shfl_down_sync(kFull, val, off);
+        if (lane + off <= last) val = max(val, o);
+    }
+    return __shfl_sync(kFull, val, first);
+}
+
+__device__ __forceinline__ int seg_min(int val, int lane, int first, int last)
+{
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int o = __shfl_down_sync(kFull, val, off);
+        if (lane + off <= last) val = min(val, o);
+    }
+    return __shfl_sync(kFull, val, first);
+}
+
+__device__ __forceinline__ long long warp_sum_ll(long long v)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(kFull, v, off);
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// decoupled look-back (executed by one full warp)
+// ---------------------------------------------------------------------------
+__device__ long long lookback_prefix(unsigned long long *status, long long t, unsigned epoch,
+                                     long long D, int lane, Ctl *ctl)
+{
+    if (t == 0) {
+        if (lane == 0) st_relaxed_u64(&status[0], pack_status(2, epoch, (unsigned long long)D));
+        return 0;
+    }
+    if (lane == 0) st_relaxed_u64(&status[t], pack_status(1, epoch, (unsigned long long)D));
+    const unsigned ep = epoch & kEpochMask;
+    long long P = 0;
+    long long j = t - 1;
+    for (;;) {
+        const long long jj = j - lane;
+        unsigned long long w;
+        unsigned state;
+        if (jj >= 0) {
+            long long spins = 0;
+            unsigned ns = 32;
+            for (;;) {
+                w = ld_relaxed_u64(&status[jj]);
+                state = (unsigned)(w >> kStateShift);
+                if (state != 0 && (unsigned)((w >> kEpochShift) & kEpochMask) == ep) break;
+                // give up after kSpinLimit polls, or at once when another wait already gave up
+                if (++spins > kSpinLimit || *((volatile int *)&ctl->err)) {
+                    atomicOr(&ctl->err, kErrLookback);
+                    state = 2;
+                    w = 0;
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 1024) ns <<= 1;
+            }
+        } else {
+            state = 2;
+            w = 0;
+        }
+        const unsigned pm = __ballot_sync(kFull, state == 2);
+        const int lim = pm ? (__ffs(pm) - 1) : 31;
+        long long val = (lane <= lim) ? (long long)(w & kValueMask) : 0;
+        P += warp_sum_ll(val);
+        if (pm) break;
+        j -= 32;
+    }
+    if (lane == 0) st_relaxed_u64(&status[t], pack_status(2, epoch, (unsigned long long)(P + D)));
+    return P;
+}
+
+// ---------------------------------------------------------------------------
+// warp-level queries used for tied vertices that the per-vertex summary cannot decide
+// ---------------------------------------------------------------------------
+
+// Vertex of degree <= 32 whose labels occupy lanes [0, deg) of the warp.
+struct WarpSmallQuery {
+    bool cand;
+    int rk;
+    __device__ int first_ge(int64_t x)
+    {
+        int m = __reduce_min_sync(kFull, (cand && rk >= x) ? rk : INT_MAX);
+        return m == INT_MAX ? -1 : m;
+    }
+    __device__ int last_lt(int64_t y)
+    {
+        return __reduce_max_sync(kFull, (cand && rk < y) ? rk : -1);
+    }
+    __device__ int tile_pick(int64_t lo)
+    {
+        const bool in = cand && rk >= lo && rk < lo + kTile;
+        const int key = __reduce_max_sync(kFull, in ? tile_priority(rk - lo) : -1);
+        const unsigned m = __ballot_sync(kFull, in && tile_priority(rk - lo) == key);
+        return m ? __shfl_sync(kFull, rk, __ffs(m) - 1) : -1;
+    }
+};
+
+// Open-addressed table region (keys/counts) of one vertex, scanned by one warp.
+// hist: 256 ints of warp-private shared memory.
+struct WarpTableQuery {
+    const uint32_t *key;
+    const uint32_t *cnt;
+    int cap;
+    int d, W, rmin, rmax;
+    int *hist;
+    int lane;
+    uint32_t *scratch;  // kPickScratch entries for tile_pick (only vertices with >= kTile distinct labels)
+
+    // x-th smallest key (0-based) among the occupied slots
+    __device__ uint32_t select(int x)
+    {
+        uint32_t prefix = 0;
+        int remaining = x;
+        for (int shift = 24; shift >= 0; shift -= 8) {
+            for (int b = lane; b < 256; b += 32) hist[b] = 0;
+            __syncwarp();
+            const uint32_t hi_mask = (shift == 24) ? 0u : (0xFFFFFFFFu << (shift + 8));
+            for (int s = lane; s < cap; s += 32) {
+                uint32_t k = key[s];
+                if (k != kEmpty && (k & hi_mask) == (prefix & hi_mask)) atomicAdd(&hist[(k >> shift) & 255], 1);
+            }
+            __syncwarp();
+            int c[8];
+            int local = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                c[i] = hist[lane * 8 + i];
+                local += c[i];
+            }
+            int incl = local;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                int o = __shfl_up_sync(kFull, incl, off);
+                if (lane >= off) incl += o;
+            }
+            const int excl = incl - local;
+            // the bin holding the target lies in the lane whose range covers `remaining`
+            const bool mine = remaining >= excl && remaining < incl;
+            const unsigned who = __ballot_sync(kFull, mine);
+            const int src = who ? (__ffs(who) - 1) : 31;
+            int digit = 0, before = 0;
+            if (lane == src) {
+                int acc = excl;
+                int i = 0;
+                for (; i < 7; ++i) {
+                    if (remaining < acc + c[i]) break;
+                    acc += c[i];
+                }
+                digit = lane * 8 + i;
+                before = acc;
+            }
+            digit = __shfl_sync(kFull, digit, src);
+            before = __shfl_sync(kFull, before, src);
+            prefix |= (uint32_t)digit << shift;
+            remaining -= before;
+            __syncwarp();
+        }
+        return prefix;
+    }
+    __device__ int rank_of(uint32_t c)
+    {
+        int n = 0;
+        for (int s = lane; s < cap; s += 32) {
+            uint32_t k = key[s];
+            n += (k != kEmpty && k < c);
+        }
+        return __reduce_add_sync(kFull, n);
+    }
+    __device__ int first_ge(int64_t x)
+    {
+        if (x >= d) return -1;
+        if (x <= rmin) return rmin;
+        const uint32_t L = select((int)x);
+        uint32_t best = kEmpty;
+        for (int s = lane; s < cap; s += 32) {
+            uint32_t k = key[s];
+            if (k != kEmpty && (int)cnt[s] == W && k >= L && k < best) best = k;
+        }
+        best = __reduce_min_sync(kFull, best);
+        if (best == kEmpty) return -1;
+        return rank_of(best);
+    }
+    __device__ int last_lt(int64_t y)
+    {
+        if (y > rmax) return rmax;
+        if (y <= rmin) return -1;
+        const uint32_t L = select((int)y);
+        int best = -1;
+        for (int s = lane; s < cap; s += 32) {
+            uint32_t k = key[s];
+            if (k != kEmpty && (int)cnt[s] == W && k < L && (int)k > best) best = (int)k;
+        }
+        best = __reduce_max_sync(kFull, best);
+        if (best < 0) return -1;
+        return rank_of((uint32_t)best);
+    }
+    __device__ uint32_t count_of(uint32_t k) const
+    {
+        uint32_t h = hslot(k, (uint32_t)cap);
+        for (int probes = 0; probes < cap; ++probes) {
+            const uint32_t x = key[h];
+            if (x == k) return cnt[h];
+            if (x == kEmpty) return 0;
+            h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
+        }
+        return 0;
+    }
+    // Sort the tile's kTile distinct labels (ranks [lo, lo + kTile)) in scratch and
+    // pick the candidate of highest tile_priority.
+    __device__ int tile_pick(int64_t lo)
+    {
+        if (!scratch) return -1;
+        const uint32_t Llo = select((int)lo);
+        const uint32_t Lhi = (lo + kTile < d) ? select((int)(lo + kTile)) : kEmpty;
+        int base = 0;
+        for (int s0 = 0; s0 < cap; s0 += 32) {
+            const int s = s0 + lane;
+            const uint32_t k = (s < cap) ? key[s] : kEmpty;
+            const bool in = k != kEmpty && k >= Llo && k < Lhi;
+            const unsigned m = __ballot_sync(kFull, in);
+            if (in && base + __popc(m & ((1u << lane) - 1)) < kPickScratch)
+                scratch[base + __popc(m & ((1u << lane) - 1))] = k;
+            base += __popc(m);
+        }
+        const int nin = min(base, kPickScratch);
+        for (int i = nin + lane; i < kPickScratch; i += 32) scratch[i] = kEmpty;
+        __syncwarp();
+        for (int kk = 2; kk <= kPickScratch; kk <<= 1) {
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                for (int i = lane; i < kPickScratch; i += 32) {
+                    const int ixj = i ^ j;
+                    if (ixj > i) {
+                        const uint32_t x = scratch[i], y = scratch[ixj];
+                        const bool up = (i & kk) == 0;
+                        if ((x > y) == up) {
+                            scratch[i] = y;
+                            scratch[ixj] = x;
+                        }
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        int best = -1, bi = -1;
+        for (int i = lane; i < nin; i += 32) {
+            if ((int)count_of(scratch[i]) == W && tile_priority(i) > best) {
+                best = tile_priority(i);
+                bi = i;
+            }
+        }
+        const int top = __reduce_max_sync(kFull, best);
+        const unsigned m = __ballot_sync(kFull, best == top && bi >= 0);
+        if (top < 0 || !m) return -1;
+        return (int)lo + __shfl_sync(kFull, bi, __ffs(m) - 1);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// the tile kernel
+// ---------------------------------------------------------------------------
+struct TileSmem {
+    int32_t lab[kTileSlots];
+    uint32_t hkey[2 * kTileSlots];
+    uint32_t hcnt[2 * kTileSlots];
+    int16_t svid[kTileSlots];
+    int64_t voff[kTileV + 1];
+    uint16_t vpos[kTileV];
+    int32_t vd[kTileV];
+    int32_t vW[kTileV];
+    int32_t vk[kTileV];
+    int32_t vcmin[kTileV];
+    int32_t vcmax[kTileV];
+    int32_t vrmin[kTileV];
+    int32_t vrmax[kTileV];
+    int32_t vpref[kTileV];
+    int32_t hard[kTileV];
+    int32_t hard_rank[kTileV];
+    int32_t hist[kNW][256];
+    int32_t wtmp[kNW];
+    long long tile;
+    long long P;
+    long long N;
+    int D;
+    int nhard;
+};
+
+__device__ __forceinline__ int vdeg(const TileSmem &S, int i) { return (int)(S.voff[i + 1] - S.voff[i]); }
+
+__global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
+    if (!ctl_active(p.ctl)) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned long long changes = 0;
+
+    for (;;) {
+        if (tid == 0) S.tile = (long long)atomicAdd(&p.ctl->ticket, 1ull);
+        __syncthreads();
+        const long long t = S.tile;
+        if (t >= p.ntiles) break;
+        const int v0 = p.tile_v0[t], v1 = p.tile_v0[t + 1];
+        const int bi = p.tile_big[t];
+
+        if (bi >= 0) {
+            // single big vertex: its distinct count was computed by big_insert
+            if (warp == 0) {
+                const long long D = p.bstat[bi].d;
+                long long P = lookback_prefix(p.status, t, p.epoch, D, lane, p.ctl);
+                if (lane == 0) {
+                    p.big_a[bi] = P;
+                    if (v0 == p.last_v) p.ctl->N = P + D;
+                }
+            }
+            __syncthreads();
+            continue;
+        }
+
+        const int nv = v1 - v0;
+        const int used = p.tile_used[t];
+        // P1: per-vertex metadata
+        for (int i = tid; i <= nv; i += kTB) S.voff[i] = p.off[v0 + i];
+        for (int i = tid; i < nv; i += kTB) {
+            S.vpos[i] = p.vpos[v0 + i];
+            S.vd[i] = 0;
+            S.vW[i] = 0;
+            S.vk[i] = 0;
+            S.vcmin[i] = INT_MAX;
+            S.vcmax[i] = -1;
+            S.vrmin[i] = 0;
+            S.vrmax[i] = 0;
+        }
+        for (int s = tid; s < used; s += kTB) S.svid[s] = -1;
+        for (int s = tid; s < 2 * used; s += kTB) {
+            S.hkey[s] = kEmpty;
+            S.hcnt[s] = 0;
+        }
+        if (tid == 0) S.nhard = 0;
+        __syncthreads();
+        // P2: slot -> vertex map (vertex starts, then an inclusive max-scan)
+        for (int i = tid; i < nv; i += kTB)
+            if (S.voff[i + 1] > S.voff[i]) S.svid[S.vpos[i]] = (int16_t)i;
+        __syncthreads();
+        {
+            constexpr int PER = kTileSlots / kTB;
+            const int s0 = tid * PER;
+            int run = -1;
+            int loc[PER];
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                int x = (s0 + i < used) ? S.svid[s0 + i] : -1;
+                run = max(run, x);
+                loc[i] = run;
+            }
+            int incl = run;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                int o = __shfl_up_sync(kFull, incl, off);
+                if (lane >= off) incl = max(incl, o);
+            }
+            if (lane == 31) S.wtmp[warp] = incl;
+            __syncthreads();
+            int carry = -1;
+            for (int w = 0; w < warp; ++w) carry = max(carry, S.wtmp[w]);
+            int up = __shfl_up_sync(kFull, incl, 1);
+            if (lane > 0) carry = max(carry, up);
+#pragma unroll
+            for (int i = 0; i < PER; ++i)
+                if (s0 + i < used) S.svid[s0 + i] = (int16_t)max(loc[i], carry);
+        }
+        __syncthreads();
+        // P3: gather labels; insert the labels of vertices with degree > 32 into their hash region
+        for (int s = tid; s < used; s += kTB) {
+            const int v = S.svid[s];
+            if (v < 0) continue;
+            const int64_t o = S.voff[v];
+            const int deg = (int)(S.voff[v + 1] - o);
+            const int j = s - (int)S.vpos[v];
+            if (j >= deg) continue;
+            const int32_t L = __ldg(&p.lab_in[__ldg(&p.nbr[o + j])]);
+            S.lab[s] = L;
+            if (deg > kSmallMax) {
+                const uint32_t cap = 2u * (uint32_t)pad32(deg);
+                const uint32_t base = 2u * (uint32_t)S.vpos[v];
+                uint32_t h = hslot((uint32_t)L, cap);
+                for (;;) {
+                    uint32_t prev = atomicCAS(&S.hkey[base + h], kEmpty, (uint32_t)L);
+                    if (prev == kEmpty || prev == (uint32_t)L) {
+                        atomicAdd(&S.hcnt[base + h], 1u);
+                        break;
+                    }
+                    h = (h + 1 == cap) ? 0 : h + 1;
+                }
+            }
+        }
+        __syncthreads();
+        // P4: counting summaries per pack of 32 slots
+        const int npk = (used + 31) >> 5;
+        for (int pass = 0; pass < 3; ++pass) {
+            for (int pk = warp; pk < npk; pk += kNW) {
+                const int s = pk * 32 + lane;
+                const int v = (s < used) ? S.svid[s] : -1;
+                const int vl0 = __shfl_sync(kFull, v, 0);
+                bool mid = false;
+                if (vl0 >= 0) {
+                    const int dg = vdeg(S, vl0);
+                    mid = dg > kSmallMax && (pk * 32 - (int)S.vpos[vl0]) < pad32(dg);
+                }
+                if (mid) {
+                    const int h0 = pk * 64 + lane, h1 = h0 + 32;
+                    const uint32_t k0 = S.hkey[h0], k1 = S.hkey[h1];
+                    const int c0 = (int)S.hcnt[h0], c1 = (int)S.hcnt[h1];
+                    if (pass == 0) {
+                        int dp = (k0 != kEmpty) + (k1 != kEmpty);
+                        int wp = max(c0, c1);
+                        dp = __reduce_add_sync(kFull, dp);
+                        wp = __reduce_max_sync(kFull, wp);
+                        if (lane == 0) {
+                            atomicAdd(&S.vd[vl0], dp);
+                            atomicMax(&S.vW[vl0], wp);
+                        }
+                    } else if (pass == 1) {
+                        const int W = S.vW[vl0];
+                        const bool q0 = k0 != kEmpty && c0 == W, q1 = k1 != kEmpty && c1 == W;
+                        int kp = (int)q0 + (int)q1;
+                        int mn = min(q0 ? (int)k0 : INT_MAX, q1 ? (int)k1 : INT_MAX);
+                        int mx = max(q0 ? (int)k0 : -1, q1 ? (int)k1 : -1);
+                        kp = __reduce_add_sync(kFull, kp);
+                        mn = __reduce_min_sync(kFull, mn);
+                        mx = __reduce_max_sync(kFull, mx);
+                        if (lane == 0) {
+                            atomicAdd(&S.vk[vl0], kp);
+                            atomicMin(&S.vcmin[vl0], mn);
+                            atomicMax(&S.vcmax[vl0], mx);
+                        }
+                    } else {
+                        const int cmn = S.vcmin[vl0], cmx = S.vcmax[vl0];
+                        int a0 = (k0 != kEmpty && (int)k0 < cmn) + (k1 != kEmpty && (int)k1 < cmn);
+                        int a1 = (k0 != kEmpty && (int)k0 < cmx) + (k1 != kEmpty && (int)k1 < cmx);
+                        a0 = __reduce_add_sync(kFull, a0);
+                        a1 = __reduce_add_sync(kFull, a1);
+                        if (lane == 0) {
+                            atomicAdd(&S.vrmin[vl0], a0);
+                            atomicAdd(&S.vrmax[vl0], a1);
+                        }
+                    }
+                } else if (pass == 0) {
+                    bool valid = false;
+                    int lab = 0;
+                    if (v >= 0) valid = (s - (int)S.vpos[v]) < vdeg(S, v);
+                    if (valid) lab = S.lab[s];
+                    const unsigned long long key =
+                        valid ? (((unsigned long long)(unsigned)v << 32) | (unsigned)lab) : (0xFFFFFFFF00000000ull | (unsigned)lane);
+                    const unsigned eq = __match_any_sync(kFull, key);
+                    const unsigned vm = __match_any_sync(kFull, valid ? v : (-1 - lane));
+                    const int cnt = __popc(eq);
+                    const bool leader = valid && ((__ffs(eq) - 1) == lane);
+                    const unsigned lm = __ballot_sync(kFull, leader);
+                    const int first = __ffs(vm) - 1, last = 31 - __clz(vm);
+                    const int W = seg_max(valid ? cnt : 0, lane, first, last);
+                    const bool cand = leader && cnt == W;
+                    const unsigned cm = __ballot_sync(kFull, cand);
+                    const int k = __popc(cm & vm);
+                    const int d = __popc(lm & vm);
+                    const int cmin = seg_min(cand ? lab : INT_MAX, lane, first, last);
+                    const int cmax = seg_max(cand ? lab : -1, lane, first, last);
+                    const int rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
+                    const int rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
+                    if (valid && lane == first) {
+                        S.vd[v] = d;
+                        S.vW[v] = W;
+                        S.vk[v] = k;
+                        S.vcmin[v] = cmin;
+                        S.vcmax[v] = cmax;
+                        S.vrmin[v] = rmin;
+                        S.vrmax[v] = rmax;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // P5: exclusive scan of distinct counts over the tile's vertices
+        {
+            const int i0 = 2 * tid, i1 = 2 * tid + 1;
+            const int x0 = i0 < nv ? S.vd[i0] : 0, x1 = i1 < nv ? S.vd[i1] : 0;
+            const int sum = x0 + x1;
+            int incl = sum;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                int o = __shfl_up_sync(kFull, incl, off);
+                if (lane >= off) incl += o;
+            }
+            if (lane == 31) S.wtmp[warp] = incl;
+            __syncthreads();
+            int base = 0, tot = 0;
+            for (int w = 0; w < kNW; ++w) {
+                if (w < warp) base += S.wtmp[w];
+                tot += S.wtmp[w];
+            }
+            const int excl = base + incl - sum;
+            if (i0 < nv) S.vpref[i0] = excl;
+            if (i1 < nv) S.vpref[i1] = excl + x0;
+            if (tid == 0) S.D = tot;
+        }
+        __syncthreads();
+        // P6: run base of the tile
+        if (warp == 0) {
+            const long long P = lookback_prefix(p.status, t, p.epoch, S.D, lane, p.ctl);
+            if (lane == 0) {
+                S.P = P;
+                if (p.last_v >= v0 && p.last_v < v1) {
+                    S.N = P + S.D;
+                    p.ctl->N = P + S.D;
+                } else {
+                    S.N = -1;
+                }
+            }
+        }
+        __syncthreads();
+        // P7: resolve from the summaries
+        for (int i = tid; i < nv; i += kTB) {
+            const int v = v0 + i;
+            const int32_t old = p.lab_in[v];
+            int32_t nl = old;
+            if (vdeg(S, i) > 0) {
+                const int k = S.vk[i];
+                if (k == 1) {
+                    nl = S.vcmin[i];
+                } else {
+                    const int d = S.vd[i];
+                    SummaryQuery q(k, d, S.vrmin[i], S.vrmax[i]);
+                    const int r = resolve_rank(S.P + S.vpref[i], d, S.N, v == p.last_v, q);
+                    if (!q.fail && r == S.vrmin[i]) {
+                        nl = S.vcmin[i];
+                    } else if (!q.fail && r == S.vrmax[i]) {
+                        nl = S.vcmax[i];
+                    } else {
+                        const int h = atomicAdd(&S.nhard, 1);
+                        S.hard[h] = i;
+                        S.hard_rank[h] = q.fail ? -1 : r;
+                        continue;
+                    }
+                }
+            }
+            p.lab_out[v] = nl;
+            changes += (nl != old);
+        }
+        __syncthreads();
+        // P8: tied vertices that need the full candidate ranks
+        for (int h = warp; h < S.nhard; h += kNW) {
+            const int i = S.hard[h];
+            int r = S.hard_rank[h];
+            const int v = v0 + i;
+            const int deg = vdeg(S, i);
+            const int d = S.vd[i], W = S.vW[i];
+            const long long a = S.P + S.vpref[i];
+            const bool is_last = v == p.last_v;
+            int32_t label;
+            if (deg <= kSmallMax) {
+                const int pos = S.vpos[i];
+                const bool valid = lane < deg;
+                const int lab = valid ? S.lab[pos + lane] : 0;
+                const unsigned key = valid ? (unsigned)lab : (0x80000000u | (unsigned)lane);
+                const unsigned eq = __match_any_sync(kFull, key);
+                const int cnt = __popc(eq);
+                const bool leader = valid && ((__ffs(eq) - 1) == lane);
+                int rk = 0;
+                for (int j = 0; j < deg; ++j) {
+                    const int lj = __shfl_sync(kFull, lab, j);
+                    const bool ldj = __shfl_sync(kFull, leader, j);
+                    rk += (ldj && lj < lab);
+                }
+                WarpSmallQuery q{leader && cnt == W, rk};
+                if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
+                const unsigned m = __ballot_sync(kFull, leader && rk == r);
+                label = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : 0);
+            } else {
+                WarpTableQuery q{&S.hkey[2 * S.vpos[i]], &S.hcnt[2 * S.vpos[i]], 2 * pad32(deg), d, W,
+                                 S.vrmin[i], S.vrmax[i], S.hist[warp], lane, nullptr};
+                if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
+                label = (r == S.vrmin[i]) ? S.vcmin[i] : (r == S.vrmax[i]) ? S.vcmax[i] : (int32_t)q.select(r);
+            }
+            if (lane == 0) {
+                const int32_t old = p.lab_in[v];
+                p.lab_out[v] = label;
+                changes += (label != old);
+            }
+        }
+        __syncthreads();
+    }
+    // one global update of the change counter per CTA
+    unsigned long long c = changes;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(kFull, c, off);
+    if (lane == 0 && c) atomicAdd(&p.ctl->changes, c);
+}
+
+// ---------------------------------------------------------------------------
+// big vertices
+// ---------------------------------------------------------------------------
+
+// Count the labels of one chunk of a big vertex's edges in shared memory, then merge
+// the distinct (label, count) pairs into the vertex's global table.
+__global__ void __launch_bounds__(kTB) big_insert_kernel(IterArgs p)
+{
+    __shared__ uint32_t skey[2 * kBigChunk];
+    __shared__ uint32_t scnt[2 * kBigChunk];
+    __shared__ int snew;
+    if (!ctl_active(p.ctl)) return;
+    const int c = blockIdx.x;
+    if (c >= p.nchunks) return;
+    const int bi = p.chunk_big[c];
+    const int64_t e0 = p.chunk_e0[c], e1 = p.chunk_e1[c];
+    const uint32_t cap = 2u * kBigChunk;
+    for (int s = threadIdx.x; s < (int)cap; s += kTB) {
+        skey[s] = kEmpty;
+        scnt[s] = 0;
+    }
+    if (threadIdx.x == 0) snew = 0;
+    __syncthreads();
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += kTB) {
+        const uint32_t L = (uint32_t)__ldg(&p.lab_in[__ldg(&p.nbr[e])]);
+        uint32_t h = hslot(L, cap);
+        for (;;) {
+            uint32_t prev = atomicCAS(&skey[h], kEmpty, L);
+            if (prev == kEmpty || prev == L) {
+                atomicAdd(&scnt[h], 1u);
+                break;
+            }
+            h = (h + 1 == cap) ? 0 : h + 1;
+        }
+    }
+    __syncthreads();
+    const int64_t toff = p.big_toff[bi];
+    const uint32_t gcap = p.big_tcap[bi];
+    uint32_t *gk = p.gkey + toff;
+    uint32_t *gc = p.gcnt + toff;
+    int fresh = 0;
+    for (int s = threadIdx.x; s < (int)cap; s += kTB) {
+        const uint32_t L = skey[s];
+        if (L == kEmpty) continue;
+        uint32_t h = hslot(L, gcap);
+        for (;;) {
+            uint32_t prev = atomicCAS(&gk[h], kEmpty, L);
+            if (prev == kEmpty || prev == L) {
+                fresh += (prev == kEmpty);
+                atomicAdd(&gc[h], scnt[s]);
+                break;
+            }
+            h = (h + 1 == gcap) ? 0 : h + 1;
+        }
+    }
+    fresh = __reduce_add_sync(kFull, fresh);
+    if ((threadIdx.x & 31) == 0 && fresh) atomicAdd(&snew, fresh);
+    __syncthreads();
+    if (threadIdx.x == 0 && snew) atomicAdd(&p.bstat[bi].d, snew);
+}
+
+// pass 0: max count; pass 1: candidates (count, min/max label); pass 2: ranks of min/max
+__global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
+{
+    __shared__ int red[3][kNW];
+    if (!ctl_active(p.ctl)) return;
+    const int c = blockIdx.x;
+    if (c >= p.nschunks) return;
+    const int bi = p.schunk_big[c];
+    const int64_t s0 = p.schunk_s0[c], s1 = p.schunk_s1[c];
+    BigStat &st = p.bstat[bi];
+    const int W = (pass >= 1) ? st.W : 0;
+    const int cmn = (pass == 2) ? st.cmin : 0, cmx = (pass == 2) ? st.cmax : 0;
+    int r0 = 0, r1 = (pass == 1) ? INT_MAX : 0, r2 = (pass == 1) ? -1 : 0;
+    for (int64_t s = s0 + threadIdx.x; s < s1; s += kTB) {
+        const uint32_t k = p.gkey[s];
+        if (k == kEmpty) continue;
+        const int cnt = (int)p.gcnt[s];
+        if (pass == 0) {
+            r0 = max(r0, cnt);
+        } else if (pass == 1) {
+            if (cnt == W) {
+                r0++;
+                r1 = min(r1, (int)k);
+                r2 = max(r2, (int)k);
+            }
+        } else {
+            r0 += (int)k < cmn;
+            r1 += (int)k < cmx;
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (pass == 0) {
+        r0 = __reduce_max_sync(kFull, r0);
+    } else if (pass == 1) {
+        r0 = __reduce_add_sync(kFull, r0);
+        r1 = __reduce_min_sync(kFull, r1);
+        r2 = __reduce_max_sync(kFull, r2);
+    } else {
+        r0 = __reduce_add_sync(kFull, r0);
+        r1 = __reduce_add_sync(kFull, r1);
+    }
+    if (lane == 0) {
+        red[0][warp] = r0;
+        red[1][warp] = r1;
+        red[2][warp] = r2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int a0 = red[0][0], a1 = red[1][0], a2 = red[2][0];
+        for (int w = 1; w < kNW; ++w) {
+            if (pass == 0) {
+                a0 = max(a0, red[0][w]);
+            } else if (pass == 1) {
+                a0 += red[0][w];
+                a1 = min(a1, red[1][w]);
+                a2 = max(a2, red[2][w]);
+            } else {
+                a0 += red[0][w];
+                a1 += red[1][w];
+            }
+        }
+        if (pass == 0) {
+            atomicMax(&st.W, a0);
+        } else if (pass == 1) {
+            if (a0) {
+                atomicAdd(&st.k, a0);
+                atomicMin(&st.cmin, a1);
+                atomicMax(&st.cmax, a2);
+            }
+        } else {
+            atomicAdd(&st.rmin, a0);
+            atomicAdd(&st.rmax, a1);
+        }
+    }
+}
+
+// One CTA per big vertex: resolve its winner (its run base is known now), write the
+// label, count the change and reset its statistics.  Warp 0 runs the queries.
+__global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
+{
+    __shared__ int hist[256];
+    extern __shared__ uint32_t pick_scratch[];  // kPickScratch entries
+    if (!ctl_active(p.ctl)) return;
+    const int bi = blockIdx.x;
+    if (bi >= p.nbig) return;
+    BigStat &st = p.bstat[bi];
+    const int v = p.big_v[bi];
+    const int lane = threadIdx.x;
+    const int k = st.k, d = st.d;
+    int32_t label;
+    if (k == 1) {
+        label = st.cmin;
+    } else {
+        const long long a = p.big_a[bi];
+        const long long N = p.ctl->N;
+        SummaryQuery sq(k, d, st.rmin, st.rmax);
+        int r = resolve_rank(a, d, N, v == p.last_v, sq);
+        if (!sq.fail && r == st.rmin) {
+            label = st.cmin;
+        } else if (!sq.fail && r == st.rmax) {
+            label = st.cmax;
+        } else {
+            WarpTableQuery q{p.gkey + p.big_toff[bi], p.gcnt + p.big_toff[bi], (int)p.big_tcap[bi], d, st.W,
+                             st.rmin, st.rmax, hist, lane, pick_scratch};
+            if (sq.fail) r = resolve_rank(a, d, N, v == p.last_v, q);
+            label = (r == st.rmin) ? st.cmin : (r == st.rmax) ? st.cmax : (int32_t)q.select(r);
+        }
+    }
+    if (lane == 0) {
+        const int32_t old = p.lab_in[v];
+        p.lab_out[v] = label;
+        if (label != old) atomicAdd(&p.ctl->changes, 1ull);
+        st.d = 0;
+        st.W = 0;
+        st.k = 0;
+        st.cmin = INT_MAX;
+        st.cmax = -1;
+        st.rmin = 0;
+        st.rmax = 0;
+    }
+}
+
+__global__ void big_clear_kernel(uint32_t *gkey, uint32_t *gcnt, int64_t nslots, const Ctl *ctl)
+{
+    if (!ctl_active(ctl)) return;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nslots; s += (int64_t)gridDim.x * blockDim.x) {
+        gkey[s] = kEmpty;
+        gcnt[s] = 0;
+    }
+}
+
+// End of an iteration: record the change count, apply the early exit
+// (DPPBase::run, dpp.cuh:83-90: break once count <= n * 1e-5) and reset the
+// per-launch counters.
+__global__ void finalize_kernel(Ctl *ctl)
+{
+    if (ctl->active) {
+        const unsigned long long c = ctl->changes;
+        if (ctl->iter < 64) ctl->counts[ctl->iter] = c;
+        ctl->iter += 1;
+        if ((long long)c <= ctl->thr || ctl->iter >= ctl->max_iter) ctl->active = 0;
+    }
+    ctl->changes = 0;
+    ctl->ticket = 0;
+}
+
+__global__ void init_labels_kernel(int32_t *lab, int64_t n)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        lab[i] = (int32_t)i;
+}
+
+__global__ void init_ctl_kernel(Ctl *ctl, long long thr, int max_iter)
+{
+    ctl->active = max_iter > 0;
+    ctl->iter = 0;
+    ctl->err = 0;
+    ctl->ticket = 0;
+    ctl->changes = 0;
+    ctl->N = 0;
+    ctl->thr = thr;
+    ctl->max_iter = max_iter;
+    for (int i = 0; i < 64; ++i) ctl->counts[i] = 0;
+}
+
+__global__ void init_bigstat_kernel(BigStat *b, int nbig)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbig; i += gridDim.x * blockDim.x) {
+        b[i].d = 0;
+        b[i].W = 0;
+        b[i].k = 0;
+        b[i].cmin = INT_MAX;
+        b[i].cmax = -1;
+        b[i].rmin = 0;
+        b[i].rmax = 0;
+    }
+}
+
+// Input validation on the device: offsets non-decreasing, neighbours in [0, n).
+__global__ void validate_kernel(const int64_t *off, const int32_t *nbr, int64_t n, int64_t m, int *bad)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int b = 0;
+    for (int64_t i = t0; i < n; i += stride)
+        if (off[i + 1] < off[i]) b |= 1;
+    for (int64_t e = t0; e < m; e += stride) {
+        const int32_t x = nbr[e];
+        if (x < 0 || (int64_t)x >= n) b |= 2;
+    }
+    if (b) atomicOr(bad, b);
+}
+
+}  // namespace galp

@@ -1,0 +1,121 @@
+/* galp.h -- C ABI of galp-gb300, the GB300-native label-propagation update.
+ *
+ * This is the drop-in boundary for galp's propagator interface.  Each entry point
+ * replaces a piece of the reference's C++ class hierarchy:
+ *
+ *   galp_create      LabelPropagator<V,E> constructor + policy preprocess()
+ *                    (label_propagation/include/label_propagator.h:11-34,
+ *                     src/common/incore.cuh:33-38 InCoreLP::preprocess,
+ *                     src/common/async.cuh:53-62 AsyncLP::preprocess) and the
+ *                    method*5+policy factory of src/main.cu:139-207
+ *   galp_run         LabelPropagator::run(niter) -> (f1, f2)
+ *                    (src/dpp/dpp.cuh:64-102 DPPBase::run)
+ *   galp_get_labels  LabelPropagator::get_labels() (include/label_propagator.h:25-29)
+ *   galp_destroy     postprocess() + destructor (src/common/incore.cuh:51-55)
+ *   galp_run_batch   no reference counterpart: clusters many independent graphs
+ *
+ * All arguments are plain pointers and sizes.  The library never calls exit();
+ * every entry point returns a status (0 = OK, negative = error, see galp_strerror).
+ *
+ * Semantics: every method/policy computes galp's method-0 ("DPP") update exactly:
+ * each vertex takes the most frequent neighbour label; ties are broken by the
+ * reference's segmented arg-max, which depends on the run's global position in the
+ * sorted run array (src/common/segmented_reduce.cuh).  Method 1 (the reference's
+ * lock-free hash path, src/lfht/) is racy and non-deterministic in the reference;
+ * here method 1 selects the hash-based counting kernels and yields the same labels
+ * as method 0.  The per-iteration change count is exact (the reference's
+ * update_labels counter, src/dpp/kernel.cuh:95-119, reads its shared counter
+ * without a barrier and may undercount).  Vertices without neighbours keep their
+ * label (the reference's update is undefined for them).
+ */
+#ifndef GALP_H
+#define GALP_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GALP_OK = 0,
+    GALP_EINVAL = -1,      /* bad argument or option */
+    GALP_ENOMEM = -2,      /* device or pinned host allocation failed */
+    GALP_ECUDA = -3,       /* CUDA runtime error */
+    GALP_ETIMEOUT = -4,    /* a device-side wait gave up (watchdog); results invalid */
+    GALP_EFORMAT = -5,     /* malformed graph (offsets not monotone, neighbour out of range) */
+    GALP_EUNSUPPORTED = -6,/* method/policy combination not provided */
+    GALP_ENODEV = -7,      /* no CUDA device */
+    GALP_EBATCH = -8       /* out-of-core: a vertex has 2^buffer_pow or more edges */
+};
+
+/* Host CSR.  offsets[n+1] (offsets[0] == 0), neighbors[m] with values in [0, n).
+ * The caller owns both arrays; for out-of-core policies they must outlive the context. */
+typedef struct {
+    const int32_t *neighbors;
+    const int64_t *offsets;
+    int64_t n;
+    int64_t m;
+} galp_csr;
+
+typedef struct {
+    int32_t method;       /* 0 = data-parallel primitives, 1 = lock-free hash (main.cu:114) */
+    int32_t policy;       /* 0 = in-core, 1 = out-of-core, 2 = out-of-core with overlap */
+    int32_t lfht_policy;  /* -l (main.cu:98-100); reported only */
+    int32_t buffer_pow;   /* -b: out-of-core batch buffer 2^buffer_pow edges (main.cu:86-88) */
+    int32_t frontier;     /* 1 = skip vertices whose neighbourhood and run base did not change */
+    int32_t dispatch;     /* 0 = fixed thresholds, 1 = learned dispatcher */
+    int32_t device;       /* CUDA device ordinal */
+    int32_t early_exit;   /* 1 = stop when changes <= n * 1e-5 (dpp.cuh:88); 0 = run niter */
+} galp_opts;
+
+#define GALP_MAX_ITERS 64
+
+typedef struct {
+    double f1;                  /* main loop + final labels to host, seconds (dpp.cuh:78-96) */
+    double f2;                  /* f1 + preprocess (allocation, upload), seconds */
+    double device_ms;           /* device time of the iteration loop (CUDA events) */
+    int32_t iters_run;          /* iterations executed (<= niter) */
+    int32_t err;                /* device error bits (0 = none) */
+    int64_t updates[GALP_MAX_ITERS]; /* labels changed per iteration */
+    int64_t runs_last;          /* runs (distinct labels summed over vertices) in the last iteration */
+    int64_t h2d_bytes;          /* bytes copied host -> device by this run */
+    int64_t d2h_bytes;          /* bytes copied device -> host by this run */
+} galp_stats;
+
+typedef struct galp_ctx galp_ctx;
+
+/* Default options: method 0, policy 0, lfht_policy 1, buffer_pow 24, no frontier,
+ * fixed dispatch, device 0, early exit on. */
+void galp_default_opts(galp_opts *opts);
+
+int galp_create(const galp_csr *graph, const galp_opts *opts, galp_ctx **ctx);
+/* Run up to niter iterations from labels = vertex IDs.  stats may be NULL. */
+int galp_run(galp_ctx *ctx, int32_t niter, galp_stats *stats);
+/* Copy the labels of the last run into out[n]. */
+int galp_get_labels(galp_ctx *ctx, int32_t *out, int64_t n);
+void galp_destroy(galp_ctx *ctx);
+const char *galp_strerror(int code);
+
+/* Launch on this CUDA stream (cudaStream_t passed as void*) instead of the
+ * context's own stream. */
+int galp_set_stream(galp_ctx *ctx, void *stream);
+
+/* Enqueue niter iterations from labels = vertex IDs on the context's stream and
+ * return without waiting (no host synchronisation, no copies).  Used to time the
+ * device loop; galp_run is the complete call. */
+int galp_enqueue(galp_ctx *ctx, int32_t niter);
+/* Wait for enqueued work and fill stats (iterations, counts, errors). */
+int galp_sync(galp_ctx *ctx, galp_stats *stats);
+
+/* Host-side evaluation of the tie-break closed form, for tests: winning candidate
+ * rank of a vertex with run base a, distinct count d, in a scope of N runs, given
+ * its candidate ranks cand[k] (ascending). */
+int32_t galp_debug_resolve_rank(int64_t a, int64_t d, int64_t N, int32_t is_last,
+                                const int32_t *cand, int32_t k);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

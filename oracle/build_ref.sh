@@ -1,0 +1,24 @@
+#!/usr/bin/env bash
+# Build oracle/_ref/ref_harness: the reference's own method-0 kernels
+# (label_propagation/src/dpp/kernel.cuh, src/common/segmented_reduce.cuh) and
+# host helpers (include/graph.h, src/common/outofcore.cuh), compiled from the
+# reference tree where it lies and run on the CPU through oracle/refsim/simt_shim.h.
+# Test infrastructure only.  Needs the reference tree (REF, default /root/reference);
+# exits 0 without building when it is absent.
+set -euo pipefail
+HERE="$(cd "$(dirname "$0")" && pwd)"
+REF="${GALP_REFERENCE:-/root/reference}"
+LP="$REF/label_propagation"
+if [ ! -f "$LP/src/common/segmented_reduce.cuh" ]; then
+    echo "build_ref: reference tree not found at $REF; skipping" >&2
+    exit 0
+fi
+mkdir -p "$HERE/_ref"
+# The kernels of segmented_reduce.cuh end where `struct SegmentedReducer` (host
+# launch code) begins; only that prefix is fed to the compiler, through a pipe.
+g++ -std=c++17 -O2 -w \
+    -include "$HERE/refsim/simt_shim.h" \
+    -include <(sed '/^struct SegmentedReducer/,$d' "$LP/src/common/segmented_reduce.cuh") \
+    -I "$HERE/refsim" -I "$LP/src" -I "$LP/include" \
+    "$HERE/refsim/ref_harness.cpp" -o "$HERE/_ref/ref_harness"
+echo "build_ref: built $HERE/_ref/ref_harness" >&2
