@@ -50,104 +50,125 @@ int cuda_status(cudaError_t e)
         if (e_ != cudaSuccess) return cuda_status(e_);     \
     } while (0)
 
-// Static per-graph schedule (host): tiles of consecutive vertices whose labels fit
-// kTileSlots shared-memory slots, small vertices (degree <= 32) never straddling a
-// 32-slot pack, larger ones starting on a pack boundary; vertices above
-// kTileSlots become single-vertex big tiles.
-void build_schedule(Schedule &S, int64_t n, const int64_t *off)
+// Static per-graph schedule (host).  Within every scope, consecutive vertices are
+// packed into tiles whose labels fit kTileSlots shared-memory slots (at most kTileV
+// vertices): a vertex of degree <= 32 never straddles a 32-slot pack, larger ones
+// start on a pack boundary, and vertices above kTileSlots become single-vertex big
+// tiles with a global hash table (offsets relative to the scope, so out-of-core
+// batches reuse one table area).
+void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts)
 {
+    S = Schedule();
     S.vpos.assign((size_t)n, 0);
-    S.tile_v0.clear();
-    S.tile_big.clear();
-    S.tile_used.clear();
-    S.big_v.clear();
-    S.last_v = -1;
-    int cur = 0, nvt = 0;
-    int64_t tstart = 0;
-    auto close = [&](int64_t vend) {
-        if (vend > tstart) {
-            S.tile_v0.push_back((int32_t)tstart);
-            S.tile_big.push_back(-1);
-            S.tile_used.push_back((uint16_t)cur);
-        }
-        tstart = vend;
-        cur = 0;
-        nvt = 0;
-    };
-    for (int64_t v = 0; v < n; ++v) {
-        const int64_t deg = off[v + 1] - off[v];
-        if (deg > 0) S.last_v = (int32_t)v;
-        if (deg > kTileSlots) {
-            close(v);
-            S.tile_v0.push_back((int32_t)v);
-            S.tile_big.push_back((int32_t)S.big_v.size());
-            S.tile_used.push_back(0);
-            S.big_v.push_back((int32_t)v);
-            tstart = v + 1;
-            continue;
-        }
-        auto place = [&](int c, int &pos, int &end) {
-            if (deg == 0) {
-                pos = c;
-                end = c;
-            } else if (deg <= kSmallMax) {
-                pos = ((c & 31) + (int)deg > 32) ? ((c + 31) & ~31) : c;
-                end = pos + (int)deg;
-            } else {
-                pos = (c + 31) & ~31;
-                end = pos + (((int)deg + 31) & ~31);
+    for (size_t k = 0; k + 1 < scope_starts.size(); ++k) {
+        Scope sc;
+        sc.v0 = scope_starts[k];
+        sc.v1 = scope_starts[k + 1];
+        sc.e0 = off[sc.v0];
+        sc.e1 = off[sc.v1];
+        sc.t0 = (int32_t)S.tile_big.size();
+        sc.b0 = (int32_t)S.big_v.size();
+        sc.c0 = (int32_t)S.chunk_big.size();
+        sc.s0 = (int32_t)S.schunk_big.size();
+        int cur = 0, nvt = 0;
+        int64_t tstart = sc.v0;
+        auto close = [&](int64_t vend) {
+            if (vend > tstart) {
+                S.tile_v0.push_back((int32_t)tstart);
+                S.tile_big.push_back(-1);
+                S.tile_used.push_back((uint16_t)cur);
             }
+            tstart = vend;
+            cur = 0;
+            nvt = 0;
         };
-        int pos, end;
-        place(cur, pos, end);
-        if (nvt == kTileV || end > kTileSlots) {
-            close(v);
-            place(0, pos, end);
+        int64_t toff = 0, ooff = 0;
+        for (int64_t v = sc.v0; v < sc.v1; ++v) {
+            const int64_t deg = off[v + 1] - off[v];
+            if (deg > 0) sc.last_v = (int32_t)v;
+            if (deg > kTileSlots) {
+                close(v);
+                const int32_t b = (int32_t)S.big_v.size();
+                S.tile_v0.push_back((int32_t)v);
+                S.tile_big.push_back(b);
+                S.tile_used.push_back(0);
+                S.big_v.push_back((int32_t)v);
+                uint32_t cap = 1;
+                while ((int64_t)cap < 2 * deg) cap <<= 1;
+                S.big_toff.push_back(toff);
+                S.big_tcap.push_back(cap);
+                S.big_ooff.push_back(ooff);
+                for (int64_t e = off[v]; e < off[v + 1]; e += kBigChunk) {
+                    S.chunk_big.push_back(b);
+                    S.chunk_e0.push_back(e);
+                    S.chunk_e1.push_back(std::min<int64_t>(e + kBigChunk, off[v + 1]));
+                }
+                for (int64_t i = 0; i < deg; i += kBigSlotChunk) {  // over the occupied list
+                    S.schunk_big.push_back(b);
+                    S.schunk_s0.push_back(i);
+                    S.schunk_s1.push_back(std::min<int64_t>(i + kBigSlotChunk, deg));
+                }
+                toff += cap;
+                ooff += deg;
+                S.m_big += deg;
+                tstart = v + 1;
+                continue;
+            }
+            auto place = [&](int c, int &pos, int &end) {
+                if (deg == 0) {
+                    pos = c;
+                    end = c;
+                } else if (deg <= kSmallMax) {
+                    pos = ((c & 31) + (int)deg > 32) ? ((c + 31) & ~31) : c;
+                    end = pos + (int)deg;
+                } else {
+                    pos = (c + 31) & ~31;
+                    end = pos + (((int)deg + 31) & ~31);
+                }
+            };
+            int pos, end;
+            place(cur, pos, end);
+            if (nvt == kTileV || end > kTileSlots) {
+                close(v);
+                place(0, pos, end);
+            }
+            S.vpos[(size_t)v] = (uint16_t)pos;
+            cur = end;
+            nvt++;
         }
-        S.vpos[v] = (uint16_t)pos;
-        cur = end;
-        nvt++;
+        close(sc.v1);
+        sc.nt = (int32_t)S.tile_big.size() - sc.t0;
+        sc.nb = (int32_t)S.big_v.size() - sc.b0;
+        sc.nc = (int32_t)S.chunk_big.size() - sc.c0;
+        sc.ns = (int32_t)S.schunk_big.size() - sc.s0;
+        sc.table_slots = toff;
+        sc.occ_slots = ooff;
+        S.max_table_slots = std::max(S.max_table_slots, toff);
+        S.max_occ_slots = std::max(S.max_occ_slots, ooff);
+        S.max_scope_edges = std::max(S.max_scope_edges, sc.e1 - sc.e0);
+        S.scopes.push_back(sc);
     }
-    close(n);
     S.tile_v0.push_back((int32_t)n);
-
-    // big-vertex tables and work lists
-    S.big_toff.clear();
-    S.big_tcap.clear();
-    S.chunk_big.clear();
-    S.chunk_e0.clear();
-    S.chunk_e1.clear();
-    S.schunk_big.clear();
-    S.schunk_s0.clear();
-    S.schunk_s1.clear();
-    int64_t toff = 0;
-    for (size_t b = 0; b < S.big_v.size(); ++b) {
-        const int64_t v = S.big_v[b];
-        const int64_t deg = off[v + 1] - off[v];
-        uint32_t cap = 1;
-        while ((int64_t)cap < 2 * deg) cap <<= 1;
-        S.big_toff.push_back(toff);
-        S.big_tcap.push_back(cap);
-        for (int64_t e = off[v]; e < off[v + 1]; e += kBigChunk) {
-            S.chunk_big.push_back((int32_t)b);
-            S.chunk_e0.push_back(e);
-            S.chunk_e1.push_back(std::min<int64_t>(e + kBigChunk, off[v + 1]));
-        }
-        for (int64_t s = 0; s < cap; s += kBigSlotChunk) {
-            S.schunk_big.push_back((int32_t)b);
-            S.schunk_s0.push_back(toff + s);
-            S.schunk_s1.push_back(toff + std::min<int64_t>(s + kBigSlotChunk, cap));
-        }
-        toff += cap;
-    }
-    S.table_slots = toff;
 }
 
-int64_t big_edges(const Schedule &S, const int64_t *off)
+int batch_boundaries(int64_t n, const int64_t *off, int buffer_pow, std::vector<int64_t> &bbs)
 {
-    int64_t mb = 0;
-    for (int32_t v : S.big_v) mb += off[v + 1] - off[v];
-    return mb;
+    const int64_t B = (int64_t)1 << buffer_pow;
+    const int64_t m = off[n];
+    bbs.assign(1, 0);
+    int64_t batch_offset = B;
+    while (batch_offset < m) {
+        int64_t left = 0, right = n + 1;
+        while (left < right) {
+            const int64_t mid = (left + right) / 2;
+            if (off[mid] < batch_offset) left = mid + 1; else right = mid;
+        }
+        if (left - 1 <= bbs.back()) return GALP_EBATCH;  // a vertex of degree >= 2^buffer_pow
+        bbs.push_back(left - 1);
+        batch_offset = off[left - 1] + B;
+    }
+    bbs.push_back(n);
+    return GALP_OK;
 }
 
 template <class T>
@@ -163,17 +184,58 @@ int upload(DevBuf &owner, T *&dst, const std::vector<T> &src, cudaStream_t st, i
     return GALP_OK;
 }
 
-int InCore::setup(const galp_csr &g, cudaStream_t st, int64_t &h2d)
+Engine::~Engine()
+{
+    if (copy_stream) cudaStreamSynchronize(copy_stream);
+    for (int i = 0; i < 2; ++i) {
+        if (ev_copied[i]) cudaEventDestroy(ev_copied[i]);
+        if (ev_consumed[i]) cudaEventDestroy(ev_consumed[i]);
+    }
+    if (copy_stream) cudaStreamDestroy(copy_stream);
+    if (registered) cudaHostUnregister((void *)h_nbr);
+}
+
+int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_t &h2d)
 {
     n = g.n;
     m = g.m;
-    build_schedule(sched, n, g.offsets);
-    m_big = big_edges(sched, g.offsets);
-    GALP_CUDA(b_nbr.alloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
+    policy = o.policy;
+    h_nbr = g.neighbors;
+    for (int64_t v = 0; v < n; ++v)
+        if (g.offsets[v + 1] < g.offsets[v]) return GALP_EFORMAT;
+    std::vector<int64_t> starts;
+    if (policy == 0) {
+        starts = {0, n};
+    } else {
+        if (o.buffer_pow < 1 || o.buffer_pow > 40) return GALP_EINVAL;
+        int rc = batch_boundaries(n, g.offsets, o.buffer_pow, starts);
+        if (rc) return rc;
+    }
+    build_schedule(sched, n, g.offsets, starts);
+
     GALP_CUDA(b_off.alloc(sizeof(int64_t) * (n + 1)));
-    if (m) GALP_CUDA(cudaMemcpyAsync(b_nbr.p, g.neighbors, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
     GALP_CUDA(cudaMemcpyAsync(b_off.p, g.offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
-    h2d += sizeof(int32_t) * m + sizeof(int64_t) * (n + 1);
+    h2d += sizeof(int64_t) * (n + 1);
+    if (policy == 0) {
+        GALP_CUDA(b_nbr[0].alloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
+        if (m) GALP_CUDA(cudaMemcpyAsync(b_nbr[0].p, g.neighbors, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
+        h2d += sizeof(int32_t) * m;
+    } else {
+        const size_t cap = sizeof(int32_t) * std::max<int64_t>(sched.max_scope_edges, 1);
+        GALP_CUDA(b_nbr[0].alloc(cap));
+        GALP_CUDA(b_nbr[1].alloc(cap));
+        // pin the caller's neighbours for asynchronous copies (graph.h:108-111 pins them too)
+        if (m) {
+            cudaError_t e = cudaHostRegister((void *)g.neighbors, sizeof(int32_t) * m, cudaHostRegisterPortable);
+            if (e == cudaSuccess) registered = true;
+            else (void)cudaGetLastError();  // already pinned by the caller, or not pinnable: copy as is
+        }
+        GALP_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            GALP_CUDA(cudaEventCreateWithFlags(&ev_copied[i], cudaEventDisableTiming));
+            GALP_CUDA(cudaEventCreateWithFlags(&ev_consumed[i], cudaEventDisableTiming));
+        }
+    }
     int rc;
     if ((rc = upload(b_vpos, d_vpos, sched.vpos, st, h2d))) return rc;
     if ((rc = upload(b_tile_v0, d_tile_v0, sched.tile_v0, st, h2d))) return rc;
@@ -182,6 +244,7 @@ int InCore::setup(const galp_csr &g, cudaStream_t st, int64_t &h2d)
     if ((rc = upload(b_big_v, d_big_v, sched.big_v, st, h2d))) return rc;
     if ((rc = upload(b_big_toff, d_big_toff, sched.big_toff, st, h2d))) return rc;
     if ((rc = upload(b_big_tcap, d_big_tcap, sched.big_tcap, st, h2d))) return rc;
+    if ((rc = upload(b_big_ooff, d_big_ooff, sched.big_ooff, st, h2d))) return rc;
     if ((rc = upload(b_chunk_big, d_chunk_big, sched.chunk_big, st, h2d))) return rc;
     if ((rc = upload(b_chunk_e0, d_chunk_e0, sched.chunk_e0, st, h2d))) return rc;
     if ((rc = upload(b_chunk_e1, d_chunk_e1, sched.chunk_e1, st, h2d))) return rc;
@@ -190,32 +253,37 @@ int InCore::setup(const galp_csr &g, cudaStream_t st, int64_t &h2d)
     if ((rc = upload(b_schunk_s1, d_schunk_s1, sched.schunk_s1, st, h2d))) return rc;
     GALP_CUDA(b_lab0.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
     GALP_CUDA(b_lab1.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
-    const size_t ntiles = sched.tile_big.size();
-    GALP_CUDA(b_status.alloc(sizeof(unsigned long long) * std::max<size_t>(ntiles, 1)));
-    GALP_CUDA(cudaMemsetAsync(b_status.p, 0, sizeof(unsigned long long) * std::max<size_t>(ntiles, 1), st));
+    int32_t max_nt = 1;
+    for (const Scope &sc : sched.scopes) max_nt = std::max(max_nt, sc.nt);
+    GALP_CUDA(b_status.alloc(sizeof(unsigned long long) * max_nt));
+    GALP_CUDA(cudaMemsetAsync(b_status.p, 0, sizeof(unsigned long long) * max_nt, st));
     GALP_CUDA(b_ctl.alloc(sizeof(Ctl)));
     const size_t nbig = sched.big_v.size();
     GALP_CUDA(b_bstat.alloc(sizeof(BigStat) * std::max<size_t>(nbig, 1)));
     GALP_CUDA(b_big_a.alloc(sizeof(int64_t) * std::max<size_t>(nbig, 1)));
-    GALP_CUDA(b_gkey.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.table_slots, 1)));
-    GALP_CUDA(b_gcnt.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.table_slots, 1)));
-    if (sched.table_slots) {
-        GALP_CUDA(cudaMemsetAsync(b_gkey.p, 0xFF, sizeof(uint32_t) * sched.table_slots, st));
-        GALP_CUDA(cudaMemsetAsync(b_gcnt.p, 0, sizeof(uint32_t) * sched.table_slots, st));
+    GALP_CUDA(b_gkey.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.max_table_slots, 1)));
+    GALP_CUDA(b_gcnt.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.max_table_slots, 1)));
+    GALP_CUDA(b_occ.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.max_occ_slots, 1)));
+    if (sched.max_table_slots) {
+        GALP_CUDA(cudaMemsetAsync(b_gkey.p, 0xFF, sizeof(uint32_t) * sched.max_table_slots, st));
+        GALP_CUDA(cudaMemsetAsync(b_gcnt.p, 0, sizeof(uint32_t) * sched.max_table_slots, st));
     }
     if (nbig) {
         init_bigstat_kernel<<<(unsigned)((nbig + 255) / 256), 256, 0, st>>>((BigStat *)b_bstat.p, (int)nbig);
         GALP_CUDA(cudaGetLastError());
     }
-    // validate the graph on the device before any iteration touches it
-    GALP_CUDA(b_bad.alloc(sizeof(int)));
-    GALP_CUDA(cudaMemsetAsync(b_bad.p, 0, sizeof(int), st));
-    validate_kernel<<<1024, 256, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr.p, n, m, (int *)b_bad.p);
-    GALP_CUDA(cudaGetLastError());
-    int bad = 0;
-    GALP_CUDA(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (policy == 0) {
+        // validate the resident graph before any iteration touches it
+        GALP_CUDA(b_bad.alloc(sizeof(int)));
+        GALP_CUDA(cudaMemsetAsync(b_bad.p, 0, sizeof(int), st));
+        validate_kernel<<<1024, 256, 0, st>>>((const int32_t *)b_nbr[0].p, m, n, (int *)b_bad.p);
+        GALP_CUDA(cudaGetLastError());
+        int bad = 0;
+        GALP_CUDA(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GALP_CUDA(cudaStreamSynchronize(st));
+        if (bad) return GALP_EFORMAT;
+    }
     GALP_CUDA(cudaStreamSynchronize(st));
-    if (bad) return GALP_EFORMAT;
 
     int dev = 0, sms = 0;
     GALP_CUDA(cudaGetDevice(&dev));
@@ -223,53 +291,62 @@ int InCore::setup(const galp_csr &g, cudaStream_t st, int64_t &h2d)
     GALP_CUDA(cudaFuncSetAttribute(lp_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)));
     int occ = 0;
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lp_tile_kernel, kTB, sizeof(TileSmem)));
-    tile_grid = (int)std::min<int64_t>((int64_t)std::max(occ, 1) * sms, std::max<size_t>(ntiles, 1));
+    tile_grid = std::max(occ, 1) * sms;
     return GALP_OK;
 }
 
-IterArgs InCore::args() const
+IterArgs Engine::args(const Scope &sc) const
 {
     IterArgs a{};
-    a.nbr = (const int32_t *)b_nbr.p;
     a.off = (const int64_t *)b_off.p;
     a.vpos = d_vpos;
     a.tile_v0 = d_tile_v0;
     a.tile_big = d_tile_big;
     a.tile_used = d_tile_used;
-    a.ntiles = (int32_t)sched.tile_big.size();
-    a.last_v = sched.last_v;
+    a.t0 = sc.t0;
+    a.ntiles = sc.nt;
+    a.last_v = sc.last_v;
     a.status = (unsigned long long *)b_status.p;
     a.ctl = (Ctl *)b_ctl.p;
-    a.nbig = (int32_t)sched.big_v.size();
+    a.b0 = sc.b0;
+    a.nbig = sc.nb;
     a.big_v = d_big_v;
     a.big_toff = d_big_toff;
     a.big_tcap = d_big_tcap;
+    a.big_ooff = d_big_ooff;
+    a.c0 = sc.c0;
     a.chunk_big = d_chunk_big;
     a.chunk_e0 = d_chunk_e0;
     a.chunk_e1 = d_chunk_e1;
-    a.nchunks = (int32_t)sched.chunk_big.size();
+    a.nchunks = sc.nc;
+    a.s0 = sc.s0;
     a.schunk_big = d_schunk_big;
     a.schunk_s0 = d_schunk_s0;
     a.schunk_s1 = d_schunk_s1;
-    a.nschunks = (int32_t)sched.schunk_big.size();
+    a.nschunks = sc.ns;
     a.gkey = (uint32_t *)b_gkey.p;
     a.gcnt = (uint32_t *)b_gcnt.p;
     a.bstat = (BigStat *)b_bstat.p;
     a.big_a = (int64_t *)b_big_a.p;
+    a.big_occ = (uint32_t *)b_occ.p;
+    a.nbr_shift = (policy == 0) ? 0 : sc.e0;
     return a;
 }
 
-// one iteration reading lab_in, writing lab_out
-int InCore::enqueue_iteration(cudaStream_t st, const int32_t *lab_in, int32_t *lab_out)
+// One update of one scope: reads lab_in (all vertices), writes lab_out for the scope.
+int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
+                          int32_t *lab_out)
 {
-    IterArgs a = args();
+    IterArgs a = args(sc);
+    a.nbr = nbr;
     a.lab_in = lab_in;
     a.lab_out = lab_out;
     if (++epoch > (unsigned)kEpochMask) {
         epoch = 1;
-        GALP_CUDA(cudaMemsetAsync(b_status.p, 0, sizeof(unsigned long long) * std::max<int32_t>(a.ntiles, 1), st));
+        GALP_CUDA(cudaMemsetAsync(b_status.p, 0, b_status.bytes, st));
     }
     a.epoch = epoch;
+    GALP_CUDA(cudaMemsetAsync(&((Ctl *)b_ctl.p)->ticket, 0, sizeof(unsigned long long), st));
     int e0 = -1;
     if (a.nbig) {
         if (prof.on) e0 = prof.mark(st);
@@ -277,34 +354,113 @@ int InCore::enqueue_iteration(cudaStream_t st, const int32_t *lab_in, int32_t *l
         for (int pass = 0; pass < 3; ++pass) big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a, pass);
         if (prof.on) prof.spans[1].push_back({e0, prof.mark(st)});
     }
-    if (prof.on) e0 = prof.mark(st);
-    lp_tile_kernel<<<tile_grid, kTB, sizeof(TileSmem), st>>>(a);
-    if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
+    if (a.ntiles) {
+        if (prof.on) e0 = prof.mark(st);
+        const int grid = std::min<int>(tile_grid, a.ntiles);
+        lp_tile_kernel<<<grid, kTB, sizeof(TileSmem), st>>>(a);
+        if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
+    }
     if (a.nbig) {
         if (prof.on) e0 = prof.mark(st);
         big_resolve_kernel<<<a.nbig, 32, sizeof(uint32_t) * kPickScratch, st>>>(a);
-        big_clear_kernel<<<1024, 256, 0, st>>>(a.gkey, a.gcnt, sched.table_slots, a.ctl);
+        big_clear_kernel<<<a.nschunks, kTB, 0, st>>>(a);
+        big_reset_kernel<<<(a.nbig + 255) / 256, 256, 0, st>>>(a);
         if (prof.on) prof.spans[2].push_back({e0, prof.mark(st)});
     }
-    finalize_kernel<<<1, 1, 0, st>>>(a.ctl);
     GALP_CUDA(cudaGetLastError());
     return GALP_OK;
 }
 
-int InCore::enqueue_run(cudaStream_t st, int niter, long long thr)
+int Engine::enqueue_init(cudaStream_t st, int niter, long long thr)
 {
-    int32_t *lab[2] = {(int32_t *)b_lab0.p, (int32_t *)b_lab1.p};
     if (n > 0) {
         const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
-        init_labels_kernel<<<blocks, 256, 0, st>>>(lab[0], n);
+        init_labels_kernel<<<blocks, 256, 0, st>>>((int32_t *)b_lab0.p, n);
     }
     init_ctl_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p, thr, niter);
     GALP_CUDA(cudaGetLastError());
-    for (int it = 0; it < niter; ++it) {
-        int rc = enqueue_iteration(st, lab[it & 1], lab[(it + 1) & 1]);
-        if (rc) return rc;
-    }
     return GALP_OK;
+}
+
+int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
+{
+    int32_t *lab[2] = {(int32_t *)b_lab0.p, (int32_t *)b_lab1.p};
+    int rc = enqueue_init(st, niter, thr);
+    if (rc) return rc;
+    for (int it = 0; it < niter; ++it) {
+        if ((rc = enqueue_scope(st, sched.scopes[0], (const int32_t *)b_nbr[0].p, lab[it & 1], lab[(it + 1) & 1])))
+            return rc;
+        finalize_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p);
+    }
+    GALP_CUDA(cudaGetLastError());
+    return GALP_OK;
+}
+
+// Policies 1/2 (SyncLP::iterate, sync.cuh:42-59; AsyncLP::iterate, async.cuh:65-89):
+// batches in order, each gathering from the current labels (earlier batches of the
+// iteration already applied) and committing its own labels when it is done.  Policy 2
+// copies batch j+1 on the copy stream while batch j computes; events order buffer
+// reuse.  The host waits once per iteration, for the early-exit decision.
+int Engine::run_outofcore(cudaStream_t st, int niter, long long thr)
+{
+    int32_t *cur = (int32_t *)b_lab0.p, *tmp = (int32_t *)b_lab1.p;
+    int rc = enqueue_init(st, niter, thr);
+    if (rc) return rc;
+    h2d_run = 0;
+    const int nb = (int)sched.scopes.size();
+    auto copy_batch = [&](int j, int buf, cudaStream_t s) -> int {
+        const Scope &sc = sched.scopes[(size_t)j];
+        const size_t bytes = sizeof(int32_t) * (size_t)(sc.e1 - sc.e0);
+        if (bytes) GALP_CUDA(cudaMemcpyAsync(b_nbr[buf].p, h_nbr + sc.e0, bytes, cudaMemcpyHostToDevice, s));
+        h2d_run += (int64_t)bytes;
+        return GALP_OK;
+    };
+    uint64_t q = 0;  // batch sequence number of this run
+    if (policy == 2 && nb > 0) {
+        if ((rc = copy_batch(0, 0, copy_stream))) return rc;
+        GALP_CUDA(cudaEventRecord(ev_copied[0], copy_stream));
+    }
+    for (int it = 0; it < niter; ++it) {
+        for (int j = 0; j < nb; ++j, ++q) {
+            const Scope &sc = sched.scopes[(size_t)j];
+            const int buf = (int)(q & 1);
+            if (policy == 2) {
+                const bool more = (j + 1 < nb) || (it + 1 < niter);
+                if (more) {
+                    if (q >= 1) GALP_CUDA(cudaStreamWaitEvent(copy_stream, ev_consumed[buf ^ 1], 0));
+                    if ((rc = copy_batch((j + 1 < nb) ? j + 1 : 0, buf ^ 1, copy_stream))) return rc;
+                    GALP_CUDA(cudaEventRecord(ev_copied[buf ^ 1], copy_stream));
+                }
+                GALP_CUDA(cudaStreamWaitEvent(st, ev_copied[buf], 0));
+            } else {
+                if ((rc = copy_batch(j, buf, st))) return rc;
+            }
+            const int32_t *nbr = (const int32_t *)b_nbr[buf].p;
+            if (it == 0 && sc.e1 > sc.e0) {
+                validate_batch_kernel<<<256, 256, 0, st>>>(nbr, sc.e1 - sc.e0, n, (Ctl *)b_ctl.p);
+                GALP_CUDA(cudaGetLastError());
+            }
+            if ((rc = enqueue_scope(st, sc, nbr, cur, tmp))) return rc;
+            if (sc.v1 > sc.v0)
+                GALP_CUDA(cudaMemcpyAsync(cur + sc.v0, tmp + sc.v0, sizeof(int32_t) * (sc.v1 - sc.v0),
+                                          cudaMemcpyDeviceToDevice, st));
+            if (policy == 2) GALP_CUDA(cudaEventRecord(ev_consumed[buf], st));
+        }
+        finalize_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p);
+        GALP_CUDA(cudaGetLastError());
+        int active = 0;
+        GALP_CUDA(cudaMemcpyAsync(&active, &((Ctl *)b_ctl.p)->active, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GALP_CUDA(cudaStreamSynchronize(st));
+        if (!active) break;
+    }
+    if (copy_stream) GALP_CUDA(cudaStreamSynchronize(copy_stream));
+    return GALP_OK;
+}
+
+const int32_t *Engine::final_labels(int iters) const
+{
+    if (policy != 0) return (const int32_t *)b_lab0.p;
+    return (iters & 1) ? (const int32_t *)b_lab1.p : (const int32_t *)b_lab0.p;
 }
 
 }  // namespace galp
@@ -354,7 +510,7 @@ int galp_create(const galp_csr *g, const galp_opts *o, galp_ctx **out)
         return GALP_EINVAL;
     if (g->offsets[0] != 0 || g->offsets[g->n] != g->m) return GALP_EFORMAT;
     if (opts.method < 0 || opts.method > 1) return GALP_EUNSUPPORTED;
-    if (opts.policy != 0) return GALP_EUNSUPPORTED;
+    if (opts.policy < 0 || opts.policy > 2) return GALP_EUNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GALP_ENODEV;
     if (opts.device < 0 || opts.device >= ndev) return GALP_EINVAL;
@@ -368,7 +524,7 @@ int galp_create(const galp_csr *g, const galp_opts *o, galp_ctx **out)
     const double t0 = now_s();
     GALP_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
     ctx->stream = ctx->own_stream;
-    int rc = ctx->incore.setup(*g, ctx->stream, ctx->h2d_setup);
+    int rc = ctx->eng.setup(*g, opts, ctx->stream, ctx->h2d_setup);
     if (rc) return rc;
     GALP_CUDA(cudaEventCreate(&ctx->ev0));
     GALP_CUDA(cudaEventCreate(&ctx->ev1));
@@ -395,7 +551,8 @@ int galp_enqueue(galp_ctx *ctx, int32_t niter)
     if (!ctx || niter < 0) return GALP_EINVAL;
     GALP_CUDA(cudaSetDevice(ctx->opts.device));
     GALP_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    int rc = ctx->incore.enqueue_run(ctx->stream, niter, exit_threshold(ctx));
+    int rc = ctx->eng.policy == 0 ? ctx->eng.enqueue_run_incore(ctx->stream, niter, exit_threshold(ctx))
+                                  : ctx->eng.run_outofcore(ctx->stream, niter, exit_threshold(ctx));
     if (rc) return rc;
     GALP_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->pending = true;
@@ -407,7 +564,7 @@ int galp_sync(galp_ctx *ctx, galp_stats *st)
     if (!ctx) return GALP_EINVAL;
     GALP_CUDA(cudaStreamSynchronize(ctx->stream));
     Ctl c;
-    GALP_CUDA(cudaMemcpy(&c, ctx->incore.b_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    GALP_CUDA(cudaMemcpy(&c, ctx->eng.b_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
     ctx->iters = c.iter;
     ctx->err = c.err;
     ctx->runs_last = c.N;
@@ -424,6 +581,7 @@ int galp_sync(galp_ctx *ctx, galp_stats *st)
         st->runs_last = c.N;
         for (int i = 0; i < GALP_MAX_ITERS; ++i) st->updates[i] = (int64_t)c.counts[i];
     }
+    if (c.err & kErrFormat) return GALP_EFORMAT;
     return (c.err & kErrLookback) ? GALP_ETIMEOUT : GALP_OK;
 }
 
@@ -438,7 +596,7 @@ int galp_run(galp_ctx *ctx, int32_t niter, galp_stats *st)
     if (rc && rc != GALP_ETIMEOUT) return rc;
     // final labels to the host (dpp.cuh:93)
     ctx->labels.resize((size_t)ctx->n);
-    const int32_t *src = (ctx->iters & 1) ? (const int32_t *)ctx->incore.b_lab1.p : (const int32_t *)ctx->incore.b_lab0.p;
+    const int32_t *src = ctx->eng.final_labels(ctx->iters);
     if (ctx->n) GALP_CUDA(cudaMemcpy(ctx->labels.data(), src, sizeof(int32_t) * ctx->n, cudaMemcpyDeviceToHost));
     ctx->have_labels = true;
     const double f1 = now_s() - t0;
@@ -446,7 +604,7 @@ int galp_run(galp_ctx *ctx, int32_t niter, galp_stats *st)
         *st = tmp;
         st->f1 = f1;
         st->f2 = f1 + ctx->t_pre;
-        st->h2d_bytes = ctx->h2d_setup;
+        st->h2d_bytes = ctx->h2d_setup + ctx->eng.h2d_run;
         st->d2h_bytes = (int64_t)sizeof(int32_t) * ctx->n;
     }
     return rc;
@@ -457,7 +615,7 @@ int galp_get_labels(galp_ctx *ctx, int32_t *out, int64_t n)
     if (!ctx || n != ctx->n || (!out && n > 0)) return GALP_EINVAL;
     if (!ctx->have_labels) {
         // labels of the last enqueued run, if any, else the initial labels
-        const int32_t *src = (ctx->iters & 1) ? (const int32_t *)ctx->incore.b_lab1.p : (const int32_t *)ctx->incore.b_lab0.p;
+        const int32_t *src = ctx->eng.final_labels(ctx->iters);
         GALP_CUDA(cudaStreamSynchronize(ctx->stream));
         if (n) GALP_CUDA(cudaMemcpy(out, src, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
         return GALP_OK;
@@ -481,21 +639,21 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
 {
     if (!ctx || !info) return GALP_EINVAL;
     std::memset(info, 0, sizeof(*info));
-    const galp::InCore &ic = ctx->incore;
+    const galp::Engine &E = ctx->eng;
     info->n = ctx->n;
     info->m = ctx->m;
-    info->m_big = ic.m_big;
-    info->ntiles = (int64_t)ic.sched.tile_big.size();
-    info->nbig = (int64_t)ic.sched.big_v.size();
-    info->table_slots = ic.sched.table_slots;
-    info->launches_per_iter = 2 + (info->nbig ? 6 : 0);
+    info->m_big = E.sched.m_big;
+    info->ntiles = (int64_t)E.sched.tile_big.size();
+    info->nbig = (int64_t)E.sched.big_v.size();
+    info->table_slots = E.sched.max_table_slots;
+    info->launches_per_iter = 2 + (info->nbig ? 7 : 0);
     return GALP_OK;
 }
 
 int galp_profile(galp_ctx *ctx, int32_t enable)
 {
     if (!ctx) return GALP_EINVAL;
-    ctx->incore.prof.on = enable != 0;
+    ctx->eng.prof.on = enable != 0;
     return GALP_OK;
 }
 
@@ -504,7 +662,7 @@ int galp_profile_read(galp_ctx *ctx, galp_kernel_times *out)
     if (!ctx || !out) return GALP_EINVAL;
     std::memset(out, 0, sizeof(*out));
     GALP_CUDA(cudaStreamSynchronize(ctx->stream));
-    galp::Profiler &P = ctx->incore.prof;
+    galp::Profiler &P = ctx->eng.prof;
     double *ms[3] = {&out->tile_ms, &out->big_pre_ms, &out->big_post_ms};
     int32_t *cnt[3] = {&out->tile_launches, &out->big_pre_groups, &out->big_post_groups};
     for (int g = 0; g < 3; ++g) {

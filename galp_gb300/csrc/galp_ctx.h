@@ -40,23 +40,45 @@ struct DevBuf {
     }
 };
 
+// One scope of run positions: the whole graph (policy 0) or one out-of-core batch
+// (policies 1/2; batch j = vertices [v0, v1) per OutOfCore::compute_batch_boundaries,
+// label_propagation/src/common/outofcore.cuh:38-60).
+struct Scope {
+    int64_t v0 = 0, v1 = 0;  // vertices
+    int64_t e0 = 0, e1 = 0;  // CSR entries
+    int32_t t0 = 0, nt = 0;  // tiles
+    int32_t b0 = 0, nb = 0;  // big vertices
+    int32_t c0 = 0, nc = 0;  // big insert chunks
+    int32_t s0 = 0, ns = 0;  // big stats chunks
+    int32_t last_v = -1;     // last vertex of the scope that owns runs
+    int64_t table_slots = 0; // global-table slots of the scope's big vertices
+    int64_t occ_slots = 0;   // occupied-list capacity of the scope's big vertices
+};
+
+// Static schedule of a graph (host side, built once).
 struct Schedule {
-    std::vector<uint16_t> vpos;
-    std::vector<int32_t> tile_v0;
-    std::vector<int32_t> tile_big;
-    std::vector<uint16_t> tile_used;
-    std::vector<int32_t> big_v;
-    std::vector<int64_t> big_toff;
-    std::vector<uint32_t> big_tcap;
+    std::vector<uint16_t> vpos;      // slot of each vertex in its tile
+    std::vector<int32_t> tile_v0;    // first vertex of each tile (+ sentinel)
+    std::vector<int32_t> tile_big;   // big-vertex index of single-vertex tiles, else -1
+    std::vector<uint16_t> tile_used; // slots used by each tile
+    std::vector<int32_t> big_v;      // vertex of each big entry
+    std::vector<int64_t> big_toff;   // table offset, relative to its scope
+    std::vector<uint32_t> big_tcap;  // table capacity (power of two >= 2 * degree)
+    std::vector<int64_t> big_ooff;   // occupied-list offset, relative to its scope
     std::vector<int32_t> chunk_big;
     std::vector<int64_t> chunk_e0, chunk_e1;
     std::vector<int32_t> schunk_big;
     std::vector<int64_t> schunk_s0, schunk_s1;
-    int64_t table_slots = 0;
-    int32_t last_v = -1;
+    std::vector<Scope> scopes;
+    int64_t max_table_slots = 0, max_occ_slots = 0, max_scope_edges = 0, m_big = 0;
 };
 
-void build_schedule(Schedule &S, int64_t n, const int64_t *off);
+// Build the schedule; scope_starts = first vertex of every scope, then n.
+void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts);
+
+// Batch boundaries of OutOfCore::compute_batch_boundaries (outofcore.cuh:38-60) for
+// 2^buffer_pow edges; returns GALP_EBATCH where the reference would loop forever.
+int batch_boundaries(int64_t n, const int64_t *off, int buffer_pow, std::vector<int64_t> &bbs);
 
 // CUDA events around kernel groups (enabled by galp_profile).
 struct Profiler {
@@ -80,18 +102,21 @@ struct Profiler {
     }
 };
 
-// Device state of one resident scope (the whole graph for policy 0).
-struct InCore {
+// Device state of a graph: resident CSR (policy 0) or streamed neighbours (policies 1/2).
+struct Engine {
     int64_t n = 0, m = 0;
+    int policy = 0;
+    const int32_t *h_nbr = nullptr;  // caller's host neighbours (streamed for policies 1/2)
+    bool registered = false;         // the library pinned h_nbr
     Schedule sched;
-    DevBuf b_nbr, b_off, b_vpos, b_tile_v0, b_tile_big, b_tile_used, b_big_v, b_big_toff, b_big_tcap;
-    DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1;
-    DevBuf b_lab0, b_lab1, b_status, b_ctl, b_bstat, b_big_a, b_gkey, b_gcnt, b_bad;
+    DevBuf b_nbr[2], b_off, b_vpos, b_tile_v0, b_tile_big, b_tile_used, b_big_v, b_big_toff, b_big_tcap;
+    DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff;
+    DevBuf b_lab0, b_lab1, b_status, b_ctl, b_bstat, b_big_a, b_gkey, b_gcnt, b_occ, b_bad;
     uint16_t *d_vpos = nullptr;
     int32_t *d_tile_v0 = nullptr, *d_tile_big = nullptr;
     uint16_t *d_tile_used = nullptr;
     int32_t *d_big_v = nullptr;
-    int64_t *d_big_toff = nullptr;
+    int64_t *d_big_toff = nullptr, *d_big_ooff = nullptr;
     uint32_t *d_big_tcap = nullptr;
     int32_t *d_chunk_big = nullptr;
     int64_t *d_chunk_e0 = nullptr, *d_chunk_e1 = nullptr;
@@ -99,13 +124,22 @@ struct InCore {
     int64_t *d_schunk_s0 = nullptr, *d_schunk_s1 = nullptr;
     unsigned epoch = 0;
     int tile_grid = 1;
-    int64_t m_big = 0;
     Profiler prof;
+    // out-of-core streaming
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
+    uint64_t batch_seq = 0;   // running batch counter (buffer parity)
+    int64_t h2d_run = 0;      // bytes streamed by the last run
 
-    int setup(const galp_csr &g, cudaStream_t st, int64_t &h2d);
-    IterArgs args() const;
-    int enqueue_iteration(cudaStream_t st, const int32_t *lab_in, int32_t *lab_out);
-    int enqueue_run(cudaStream_t st, int niter, long long thr);
+    ~Engine();
+    int setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_t &h2d);
+    IterArgs args(const Scope &sc) const;
+    int enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
+                      int32_t *lab_out);
+    int enqueue_run_incore(cudaStream_t st, int niter, long long thr);
+    int run_outofcore(cudaStream_t st, int niter, long long thr);
+    int enqueue_init(cudaStream_t st, int niter, long long thr);
+    const int32_t *final_labels(int iters) const;
 };
 
 }  // namespace galp
@@ -116,7 +150,7 @@ struct galp_ctx {
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    galp::InCore incore;
+    galp::Engine eng;
     double t_pre = 0;
     int64_t h2d_setup = 0;
     bool pending = false;

@@ -37,10 +37,12 @@ constexpr int kBigChunk = 4096;       // edges per big_insert CTA
 constexpr int kBigSlotChunk = 8192;   // table slots per big_stats CTA
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
+constexpr int kHardWarps = 4;         // warps of a tile CTA that resolve vertices needing full ranks
 constexpr long long kSpinLimit = 1ll << 20;  // look-back give-up bound (about a second)
 
 // error bits in Ctl::err
 constexpr int kErrLookback = 1;
+constexpr int kErrFormat = 2;
 
 struct Ctl {
     int active;                 // 1 while iterations still run
@@ -68,8 +70,14 @@ struct BigStat {
     int pad;
 };
 
+// Arguments of one iteration over one scope of run positions: the whole graph
+// (in-core) or one batch (out-of-core).  Tile, big-vertex and chunk indices are
+// relative to the scope's bases t0/b0/c0/s0; neighbour reads subtract nbr_shift
+// (the first CSR entry held by the neighbour buffer).
 struct IterArgs {
-    const int32_t *nbr;        // CSR neighbours (global IDs)
+    const int32_t *nbr;        // CSR neighbours (global IDs), entries [nbr_shift, ...)
+    int64_t nbr_shift;
+    int32_t t0, b0, c0, s0;    // scope bases: tiles, big vertices, insert chunks, stats chunks
     const int64_t *off;        // CSR offsets (global)
     const uint16_t *vpos;      // slot position of each vertex in its tile
     const int32_t *tile_v0;    // ntiles+1: first vertex of each tile
@@ -92,13 +100,15 @@ struct IterArgs {
     const int64_t *chunk_e1;    // insert chunk -> end edge
     int32_t nchunks;
     const int32_t *schunk_big;  // stats chunk -> big index
-    const int64_t *schunk_s0;   // stats chunk -> first table slot (global)
+    const int64_t *schunk_s0;   // stats chunk -> first entry of the vertex's occupied list
     const int64_t *schunk_s1;
     int32_t nschunks;
     uint32_t *gkey;             // big tables: keys
     uint32_t *gcnt;             // big tables: counts
     BigStat *bstat;
     int64_t *big_a;             // run base of each big vertex (written by the scan)
+    uint32_t *big_occ;          // occupied-slot list of each big table (capacity = degree)
+    const int64_t *big_ooff;    // offset of each big vertex's occupied list
 };
 
 __device__ __forceinline__ int pad32(int x) { return (x + 31) & ~31; }
@@ -226,6 +236,11 @@ struct WarpTableQuery {
     int *hist;
     int lane;
     uint32_t *scratch;  // kPickScratch entries for tile_pick (only vertices with >= kTile distinct labels)
+    const uint32_t *occ = nullptr;  // optional list of the occupied slots (global tables)
+    int nocc = 0;
+
+    __device__ int nslots() const { return occ ? nocc : cap; }
+    __device__ int slot(int i) const { return occ ? (int)occ[i] : i; }
 
     // x-th smallest key (0-based) among the occupied slots
     __device__ uint32_t select(int x)
@@ -236,8 +251,8 @@ struct WarpTableQuery {
             for (int b = lane; b < 256; b += 32) hist[b] = 0;
             __syncwarp();
             const uint32_t hi_mask = (shift == 24) ? 0u : (0xFFFFFFFFu << (shift + 8));
-            for (int s = lane; s < cap; s += 32) {
-                uint32_t k = key[s];
+            for (int i = lane; i < nslots(); i += 32) {
+                uint32_t k = key[slot(i)];
                 if (k != kEmpty && (k & hi_mask) == (prefix & hi_mask)) atomicAdd(&hist[(k >> shift) & 255], 1);
             }
             __syncwarp();
@@ -281,8 +296,8 @@ struct WarpTableQuery {
     __device__ int rank_of(uint32_t c)
     {
         int n = 0;
-        for (int s = lane; s < cap; s += 32) {
-            uint32_t k = key[s];
+        for (int i = lane; i < nslots(); i += 32) {
+            uint32_t k = key[slot(i)];
             n += (k != kEmpty && k < c);
         }
         return __reduce_add_sync(kFull, n);
@@ -293,7 +308,8 @@ struct WarpTableQuery {
         if (x <= rmin) return rmin;
         const uint32_t L = select((int)x);
         uint32_t best = kEmpty;
-        for (int s = lane; s < cap; s += 32) {
+        for (int i = lane; i < nslots(); i += 32) {
+            const int s = slot(i);
             uint32_t k = key[s];
             if (k != kEmpty && (int)cnt[s] == W && k >= L && k < best) best = k;
         }
@@ -307,7 +323,8 @@ struct WarpTableQuery {
         if (y <= rmin) return -1;
         const uint32_t L = select((int)y);
         int best = -1;
-        for (int s = lane; s < cap; s += 32) {
+        for (int i = lane; i < nslots(); i += 32) {
+            const int s = slot(i);
             uint32_t k = key[s];
             if (k != kEmpty && (int)cnt[s] == W && k < L && (int)k > best) best = (int)k;
         }
@@ -334,9 +351,9 @@ struct WarpTableQuery {
         const uint32_t Llo = select((int)lo);
         const uint32_t Lhi = (lo + kTile < d) ? select((int)(lo + kTile)) : kEmpty;
         int base = 0;
-        for (int s0 = 0; s0 < cap; s0 += 32) {
-            const int s = s0 + lane;
-            const uint32_t k = (s < cap) ? key[s] : kEmpty;
+        for (int i0 = 0; i0 < nslots(); i0 += 32) {
+            const int i = i0 + lane;
+            const uint32_t k = (i < nslots()) ? key[slot(i)] : kEmpty;
             const bool in = k != kEmpty && k >= Llo && k < Lhi;
             const unsigned m = __ballot_sync(kFull, in);
             if (in && base + __popc(m & ((1u << lane) - 1)) < kPickScratch)
@@ -393,21 +410,22 @@ struct TileSmem {
     int32_t vcmax[kTileV];
     int32_t vrmin[kTileV];
     int32_t vrmax[kTileV];
-    int32_t vpref[kTileV];
-    int32_t hard[kTileV];
-    int32_t hard_rank[kTileV];
-    int32_t hist[kNW][256];
+    int16_t vpref[kTileV];
+    int16_t hard[kTileV];
+    int16_t hard_rank[kTileV];
+    int32_t hist[kHardWarps][256];
     int32_t wtmp[kNW];
     long long tile;
     long long P;
     long long N;
     int D;
     int nhard;
+    int has_mid;
 };
 
 __device__ __forceinline__ int vdeg(const TileSmem &S, int i) { return (int)(S.voff[i + 1] - S.voff[i]); }
 
-__global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
+__global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
@@ -420,8 +438,9 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
         __syncthreads();
         const long long t = S.tile;
         if (t >= p.ntiles) break;
-        const int v0 = p.tile_v0[t], v1 = p.tile_v0[t + 1];
-        const int bi = p.tile_big[t];
+        const long long tg = p.t0 + t;
+        const int v0 = p.tile_v0[tg], v1 = p.tile_v0[tg + 1];
+        const int bi = p.tile_big[tg];
 
         if (bi >= 0) {
             // single big vertex: its distinct count was computed by big_insert
@@ -438,11 +457,11 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
         }
 
         const int nv = v1 - v0;
-        const int used = p.tile_used[t];
-        // P1: per-vertex metadata
-        for (int i = tid; i <= nv; i += kTB) S.voff[i] = p.off[v0 + i];
+        const int used = p.tile_used[tg];
+        // P1: per-vertex metadata, slot map and hash regions reset
+        for (int i = tid; i <= nv; i += kTB) S.voff[i] = __ldg(&p.off[v0 + i]);
         for (int i = tid; i < nv; i += kTB) {
-            S.vpos[i] = p.vpos[v0 + i];
+            S.vpos[i] = __ldg(&p.vpos[v0 + i]);
             S.vd[i] = 0;
             S.vW[i] = 0;
             S.vk[i] = 0;
@@ -452,16 +471,28 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
             S.vrmax[i] = 0;
         }
         for (int s = tid; s < used; s += kTB) S.svid[s] = -1;
-        for (int s = tid; s < 2 * used; s += kTB) {
-            S.hkey[s] = kEmpty;
-            S.hcnt[s] = 0;
+        if (tid == 0) {
+            S.nhard = 0;
+            S.has_mid = 0;
         }
-        if (tid == 0) S.nhard = 0;
         __syncthreads();
-        // P2: slot -> vertex map (vertex starts, then an inclusive max-scan)
-        for (int i = tid; i < nv; i += kTB)
-            if (S.voff[i + 1] > S.voff[i]) S.svid[S.vpos[i]] = (int16_t)i;
+        // P2: slot -> vertex map (vertex starts, then an inclusive max-scan); hash
+        // regions of vertices above 32 edges cleared
+        {
+            int mid_here = 0;
+            for (int i = tid; i < nv; i += kTB) {
+                const int dg = vdeg(S, i);
+                if (dg > 0) S.svid[S.vpos[i]] = (int16_t)i;
+                if (dg > kSmallMax) mid_here = 1;
+            }
+            if (__any_sync(kFull, mid_here) && lane == 0) S.has_mid = 1;
+        }
         __syncthreads();
+        if (S.has_mid)
+            for (int s = tid; s < 2 * used; s += kTB) {
+                S.hkey[s] = kEmpty;
+                S.hcnt[s] = 0;
+            }
         {
             constexpr int PER = kTileSlots / kTB;
             const int s0 = tid * PER;
@@ -490,34 +521,56 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
                 if (s0 + i < used) S.svid[s0 + i] = (int16_t)max(loc[i], carry);
         }
         __syncthreads();
-        // P3: gather labels; insert the labels of vertices with degree > 32 into their hash region
-        for (int s = tid; s < used; s += kTB) {
-            const int v = S.svid[s];
-            if (v < 0) continue;
-            const int64_t o = S.voff[v];
-            const int deg = (int)(S.voff[v + 1] - o);
-            const int j = s - (int)S.vpos[v];
-            if (j >= deg) continue;
-            const int32_t L = __ldg(&p.lab_in[__ldg(&p.nbr[o + j])]);
-            S.lab[s] = L;
-            if (deg > kSmallMax) {
-                const uint32_t cap = 2u * (uint32_t)pad32(deg);
-                const uint32_t base = 2u * (uint32_t)S.vpos[v];
-                uint32_t h = hslot((uint32_t)L, cap);
-                for (;;) {
-                    uint32_t prev = atomicCAS(&S.hkey[base + h], kEmpty, (uint32_t)L);
-                    if (prev == kEmpty || prev == (uint32_t)L) {
-                        atomicAdd(&S.hcnt[base + h], 1u);
-                        break;
+        // P3: gather labels with all of a thread's loads in flight together; insert
+        // the labels of vertices with degree > 32 into their hash region
+        {
+            constexpr int PER = kTileSlots / kTB;
+            int nb[PER];
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                const int s = tid + i * kTB;
+                nb[i] = -1;
+                if (s < used) {
+                    const int v = S.svid[s];
+                    if (v >= 0) {
+                        const int64_t o = S.voff[v];
+                        const int j = s - (int)S.vpos[v];
+                        if (j < (int)(S.voff[v + 1] - o)) nb[i] = __ldg(&p.nbr[o + j - p.nbr_shift]);
                     }
-                    h = (h + 1 == cap) ? 0 : h + 1;
+                }
+            }
+            int lb[PER];
+#pragma unroll
+            for (int i = 0; i < PER; ++i) lb[i] = (nb[i] >= 0) ? __ldg(&p.lab_in[nb[i]]) : -1;
+#pragma unroll
+            for (int i = 0; i < PER; ++i) {
+                if (nb[i] < 0) continue;
+                const int s = tid + i * kTB;
+                const int32_t L = lb[i];
+                S.lab[s] = L;
+                const int v = S.svid[s];
+                const int deg = vdeg(S, v);
+                if (deg > kSmallMax) {
+                    const uint32_t cap = 2u * (uint32_t)pad32(deg);
+                    const uint32_t base = 2u * (uint32_t)S.vpos[v];
+                    uint32_t h = hslot((uint32_t)L, cap);
+                    for (;;) {
+                        uint32_t prev = atomicCAS(&S.hkey[base + h], kEmpty, (uint32_t)L);
+                        if (prev == kEmpty || prev == (uint32_t)L) {
+                            atomicAdd(&S.hcnt[base + h], 1u);
+                            break;
+                        }
+                        h = (h + 1 == cap) ? 0 : h + 1;
+                    }
                 }
             }
         }
         __syncthreads();
-        // P4: counting summaries per pack of 32 slots
+        // P4: counting summaries per pack of 32 slots (passes 1 and 2 only for tiles
+        // holding a vertex above 32 edges)
         const int npk = (used + 31) >> 5;
-        for (int pass = 0; pass < 3; ++pass) {
+        const int npass = S.has_mid ? 3 : 1;
+        for (int pass = 0; pass < npass; ++pass) {
             for (int pk = warp; pk < npk; pk += kNW) {
                 const int s = pk * 32 + lane;
                 const int v = (s < used) ? S.svid[s] : -1;
@@ -555,6 +608,7 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
                             atomicMax(&S.vcmax[vl0], mx);
                         }
                     } else {
+                        if (S.vk[vl0] == 1) continue;  // a unique winner needs no ranks
                         const int cmn = S.vcmin[vl0], cmx = S.vcmax[vl0];
                         int a0 = (k0 != kEmpty && (int)k0 < cmn) + (k1 != kEmpty && (int)k1 < cmn);
                         int a1 = (k0 != kEmpty && (int)k0 < cmx) + (k1 != kEmpty && (int)k1 < cmx);
@@ -583,10 +637,17 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
                     const unsigned cm = __ballot_sync(kFull, cand);
                     const int k = __popc(cm & vm);
                     const int d = __popc(lm & vm);
-                    const int cmin = seg_min(cand ? lab : INT_MAX, lane, first, last);
-                    const int cmax = seg_max(cand ? lab : -1, lane, first, last);
-                    const int rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
-                    const int rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
+                    int cmin, cmax, rmin = 0, rmax = 0;
+                    if (__all_sync(kFull, !valid || k == 1)) {
+                        // every vertex of the pack has a unique winner: no ranks needed
+                        const unsigned m = cm & vm;
+                        cmin = cmax = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : lane);
+                    } else {
+                        cmin = seg_min(cand ? lab : INT_MAX, lane, first, last);
+                        cmax = seg_max(cand ? lab : -1, lane, first, last);
+                        rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
+                        rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
+                    }
                     if (valid && lane == first) {
                         S.vd[v] = d;
                         S.vW[v] = W;
@@ -619,12 +680,13 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
                 tot += S.wtmp[w];
             }
             const int excl = base + incl - sum;
-            if (i0 < nv) S.vpref[i0] = excl;
-            if (i1 < nv) S.vpref[i1] = excl + x0;
+            if (i0 < nv) S.vpref[i0] = (int16_t)excl;
+            if (i1 < nv) S.vpref[i1] = (int16_t)(excl + x0);
             if (tid == 0) S.D = tot;
         }
         __syncthreads();
-        // P6: run base of the tile
+        // P6: warp 0 obtains the tile's run base by look-back while the other warps
+        // write the vertices whose winner is unique (no position needed)
         if (warp == 0) {
             const long long P = lookback_prefix(p.status, t, p.epoch, S.D, lane, p.ctl);
             if (lane == 0) {
@@ -636,75 +698,81 @@ __global__ void __launch_bounds__(kTB) lp_tile_kernel(IterArgs p)
                     S.N = -1;
                 }
             }
+        } else {
+            for (int i = tid - 32; i < nv; i += kTB - 32) {
+                const int v = v0 + i;
+                if (vdeg(S, i) == 0 || S.vk[i] == 1) {
+                    const int32_t old = __ldg(&p.lab_in[v]);
+                    const int32_t nl = vdeg(S, i) == 0 ? old : S.vcmin[i];
+                    p.lab_out[v] = nl;
+                    changes += (nl != old);
+                }
+            }
         }
         __syncthreads();
-        // P7: resolve from the summaries
+        // P7: resolve tied vertices from the summaries
         for (int i = tid; i < nv; i += kTB) {
+            if (vdeg(S, i) == 0 || S.vk[i] == 1) continue;
             const int v = v0 + i;
-            const int32_t old = p.lab_in[v];
-            int32_t nl = old;
-            if (vdeg(S, i) > 0) {
-                const int k = S.vk[i];
-                if (k == 1) {
-                    nl = S.vcmin[i];
-                } else {
-                    const int d = S.vd[i];
-                    SummaryQuery q(k, d, S.vrmin[i], S.vrmax[i]);
-                    const int r = resolve_rank(S.P + S.vpref[i], d, S.N, v == p.last_v, q);
-                    if (!q.fail && r == S.vrmin[i]) {
-                        nl = S.vcmin[i];
-                    } else if (!q.fail && r == S.vrmax[i]) {
-                        nl = S.vcmax[i];
-                    } else {
-                        const int h = atomicAdd(&S.nhard, 1);
-                        S.hard[h] = i;
-                        S.hard_rank[h] = q.fail ? -1 : r;
-                        continue;
-                    }
-                }
+            const int32_t old = __ldg(&p.lab_in[v]);
+            int32_t nl;
+            const int k = S.vk[i], d = S.vd[i];
+            SummaryQuery q(k, d, S.vrmin[i], S.vrmax[i]);
+            const int r = resolve_rank(S.P + S.vpref[i], d, S.N, v == p.last_v, q);
+            if (!q.fail && r == S.vrmin[i]) {
+                nl = S.vcmin[i];
+            } else if (!q.fail && r == S.vrmax[i]) {
+                nl = S.vcmax[i];
+            } else {
+                const int h = atomicAdd(&S.nhard, 1);
+                S.hard[h] = (int16_t)i;
+                S.hard_rank[h] = (int16_t)(q.fail ? -1 : r);
+                continue;
             }
             p.lab_out[v] = nl;
             changes += (nl != old);
         }
         __syncthreads();
         // P8: tied vertices that need the full candidate ranks
-        for (int h = warp; h < S.nhard; h += kNW) {
-            const int i = S.hard[h];
-            int r = S.hard_rank[h];
-            const int v = v0 + i;
-            const int deg = vdeg(S, i);
-            const int d = S.vd[i], W = S.vW[i];
-            const long long a = S.P + S.vpref[i];
-            const bool is_last = v == p.last_v;
-            int32_t label;
-            if (deg <= kSmallMax) {
-                const int pos = S.vpos[i];
-                const bool valid = lane < deg;
-                const int lab = valid ? S.lab[pos + lane] : 0;
-                const unsigned key = valid ? (unsigned)lab : (0x80000000u | (unsigned)lane);
-                const unsigned eq = __match_any_sync(kFull, key);
-                const int cnt = __popc(eq);
-                const bool leader = valid && ((__ffs(eq) - 1) == lane);
-                int rk = 0;
-                for (int j = 0; j < deg; ++j) {
-                    const int lj = __shfl_sync(kFull, lab, j);
-                    const bool ldj = __shfl_sync(kFull, leader, j);
-                    rk += (ldj && lj < lab);
+        if (S.nhard) {
+            for (int h = warp; warp < kHardWarps && h < S.nhard; h += kHardWarps) {
+                const int i = S.hard[h];
+                int r = S.hard_rank[h];
+                const int v = v0 + i;
+                const int deg = vdeg(S, i);
+                const int d = S.vd[i], W = S.vW[i];
+                const long long a = S.P + S.vpref[i];
+                const bool is_last = v == p.last_v;
+                int32_t label;
+                if (deg <= kSmallMax) {
+                    const int pos = S.vpos[i];
+                    const bool valid = lane < deg;
+                    const int lab = valid ? S.lab[pos + lane] : 0;
+                    const unsigned key = valid ? (unsigned)lab : (0x80000000u | (unsigned)lane);
+                    const unsigned eq = __match_any_sync(kFull, key);
+                    const int cnt = __popc(eq);
+                    const bool leader = valid && ((__ffs(eq) - 1) == lane);
+                    int rk = 0;
+                    for (int j = 0; j < deg; ++j) {
+                        const int lj = __shfl_sync(kFull, lab, j);
+                        const bool ldj = __shfl_sync(kFull, leader, j);
+                        rk += (ldj && lj < lab);
+                    }
+                    WarpSmallQuery q{leader && cnt == W, rk};
+                    if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
+                    const unsigned m = __ballot_sync(kFull, leader && rk == r);
+                    label = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : 0);
+                } else {
+                    WarpTableQuery q{&S.hkey[2 * S.vpos[i]], &S.hcnt[2 * S.vpos[i]], 2 * pad32(deg), d, W,
+                                     S.vrmin[i], S.vrmax[i], S.hist[warp], lane, nullptr};
+                    if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
+                    label = (r == S.vrmin[i]) ? S.vcmin[i] : (r == S.vrmax[i]) ? S.vcmax[i] : (int32_t)q.select(r);
                 }
-                WarpSmallQuery q{leader && cnt == W, rk};
-                if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
-                const unsigned m = __ballot_sync(kFull, leader && rk == r);
-                label = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : 0);
-            } else {
-                WarpTableQuery q{&S.hkey[2 * S.vpos[i]], &S.hcnt[2 * S.vpos[i]], 2 * pad32(deg), d, W,
-                                 S.vrmin[i], S.vrmax[i], S.hist[warp], lane, nullptr};
-                if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
-                label = (r == S.vrmin[i]) ? S.vcmin[i] : (r == S.vrmax[i]) ? S.vcmax[i] : (int32_t)q.select(r);
-            }
-            if (lane == 0) {
-                const int32_t old = p.lab_in[v];
-                p.lab_out[v] = label;
-                changes += (label != old);
+                if (lane == 0) {
+                    const int32_t old = __ldg(&p.lab_in[v]);
+                    p.lab_out[v] = label;
+                    changes += (label != old);
+                }
             }
         }
         __syncthreads();
@@ -726,18 +794,16 @@ __global__ void __launch_bounds__(kTB) big_insert_kernel(IterArgs p)
 {
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
-    __shared__ int snew;
     if (!ctl_active(p.ctl)) return;
-    const int c = blockIdx.x;
-    if (c >= p.nchunks) return;
+    if ((int)blockIdx.x >= p.nchunks) return;
+    const int c = p.c0 + blockIdx.x;
     const int bi = p.chunk_big[c];
-    const int64_t e0 = p.chunk_e0[c], e1 = p.chunk_e1[c];
+    const int64_t e0 = p.chunk_e0[c] - p.nbr_shift, e1 = p.chunk_e1[c] - p.nbr_shift;
     const uint32_t cap = 2u * kBigChunk;
     for (int s = threadIdx.x; s < (int)cap; s += kTB) {
         skey[s] = kEmpty;
         scnt[s] = 0;
     }
-    if (threadIdx.x == 0) snew = 0;
     __syncthreads();
     for (int64_t e = e0 + threadIdx.x; e < e1; e += kTB) {
         const uint32_t L = (uint32_t)__ldg(&p.lab_in[__ldg(&p.nbr[e])]);
@@ -756,44 +822,61 @@ __global__ void __launch_bounds__(kTB) big_insert_kernel(IterArgs p)
     const uint32_t gcap = p.big_tcap[bi];
     uint32_t *gk = p.gkey + toff;
     uint32_t *gc = p.gcnt + toff;
-    int fresh = 0;
-    for (int s = threadIdx.x; s < (int)cap; s += kTB) {
+    uint32_t *occ = p.big_occ + p.big_ooff[bi];
+    int *dcount = &p.bstat[bi].d;
+    const int lane = threadIdx.x & 31;
+    for (int s = threadIdx.x; s < (int)cap; s += kTB) {  // cap is a multiple of kTB
         const uint32_t L = skey[s];
-        if (L == kEmpty) continue;
-        uint32_t h = hslot(L, gcap);
-        for (;;) {
-            uint32_t prev = atomicCAS(&gk[h], kEmpty, L);
-            if (prev == kEmpty || prev == L) {
-                fresh += (prev == kEmpty);
-                atomicAdd(&gc[h], scnt[s]);
-                break;
+        bool created = false;
+        uint32_t h = 0;
+        if (L != kEmpty) {
+            h = hslot(L, gcap);
+            for (;;) {
+                uint32_t prev = atomicCAS(&gk[h], kEmpty, L);
+                if (prev == kEmpty || prev == L) {
+                    created = prev == kEmpty;
+                    atomicAdd(&gc[h], scnt[s]);
+                    break;
+                }
+                h = (h + 1 == gcap) ? 0 : h + 1;
             }
-            h = (h + 1 == gcap) ? 0 : h + 1;
+        }
+        // record newly occupied slots in the vertex's occupied list (warp-aggregated)
+        const unsigned m = __ballot_sync(kFull, created);
+        if (m) {
+            int base = 0;
+            if (lane == __ffs(m) - 1) base = atomicAdd(dcount, __popc(m));
+            base = __shfl_sync(kFull, base, __ffs(m) - 1);
+            if (created) occ[base + __popc(m & ((1u << lane) - 1))] = h;
         }
     }
-    fresh = __reduce_add_sync(kFull, fresh);
-    if ((threadIdx.x & 31) == 0 && fresh) atomicAdd(&snew, fresh);
-    __syncthreads();
-    if (threadIdx.x == 0 && snew) atomicAdd(&p.bstat[bi].d, snew);
 }
 
-// pass 0: max count; pass 1: candidates (count, min/max label); pass 2: ranks of min/max
+// Over the occupied slots of each big vertex's table: pass 0 max count; pass 1
+// candidates (count, smallest and largest label); pass 2 ranks of those two labels.
 __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
 {
     __shared__ int red[3][kNW];
     if (!ctl_active(p.ctl)) return;
-    const int c = blockIdx.x;
-    if (c >= p.nschunks) return;
+    if ((int)blockIdx.x >= p.nschunks) return;
+    const int c = p.s0 + blockIdx.x;
     const int bi = p.schunk_big[c];
-    const int64_t s0 = p.schunk_s0[c], s1 = p.schunk_s1[c];
     BigStat &st = p.bstat[bi];
+    const int d = *((volatile int *)&st.d);
+    const int64_t i0 = p.schunk_s0[c];
+    const int64_t i1 = min(p.schunk_s1[c], (int64_t)d);
+    if (i0 >= i1) return;
+    if (pass == 2 && st.k == 1) return;  // a unique winner needs no ranks
+    const uint32_t *occ = p.big_occ + p.big_ooff[bi];
+    const uint32_t *gk = p.gkey + p.big_toff[bi];
+    const uint32_t *gc = p.gcnt + p.big_toff[bi];
     const int W = (pass >= 1) ? st.W : 0;
     const int cmn = (pass == 2) ? st.cmin : 0, cmx = (pass == 2) ? st.cmax : 0;
     int r0 = 0, r1 = (pass == 1) ? INT_MAX : 0, r2 = (pass == 1) ? -1 : 0;
-    for (int64_t s = s0 + threadIdx.x; s < s1; s += kTB) {
-        const uint32_t k = p.gkey[s];
-        if (k == kEmpty) continue;
-        const int cnt = (int)p.gcnt[s];
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
+        const uint32_t sidx = occ[i];
+        const uint32_t k = gk[sidx];
+        const int cnt = (int)gc[sidx];
         if (pass == 0) {
             r0 = max(r0, cnt);
         } else if (pass == 1) {
@@ -853,15 +936,15 @@ __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
     }
 }
 
-// One CTA per big vertex: resolve its winner (its run base is known now), write the
-// label, count the change and reset its statistics.  Warp 0 runs the queries.
+// One warp per big vertex: resolve its winner (its run base is known now), write the
+// label and count the change.
 __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
 {
     __shared__ int hist[256];
     extern __shared__ uint32_t pick_scratch[];  // kPickScratch entries
     if (!ctl_active(p.ctl)) return;
-    const int bi = blockIdx.x;
-    if (bi >= p.nbig) return;
+    if ((int)blockIdx.x >= p.nbig) return;
+    const int bi = p.b0 + blockIdx.x;
     BigStat &st = p.bstat[bi];
     const int v = p.big_v[bi];
     const int lane = threadIdx.x;
@@ -881,6 +964,8 @@ __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
         } else {
             WarpTableQuery q{p.gkey + p.big_toff[bi], p.gcnt + p.big_toff[bi], (int)p.big_tcap[bi], d, st.W,
                              st.rmin, st.rmax, hist, lane, pick_scratch};
+            q.occ = p.big_occ + p.big_ooff[bi];
+            q.nocc = d;
             if (sq.fail) r = resolve_rank(a, d, N, v == p.last_v, q);
             label = (r == st.rmin) ? st.cmin : (r == st.rmax) ? st.cmax : (int32_t)q.select(r);
         }
@@ -889,22 +974,41 @@ __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
         const int32_t old = p.lab_in[v];
         p.lab_out[v] = label;
         if (label != old) atomicAdd(&p.ctl->changes, 1ull);
-        st.d = 0;
-        st.W = 0;
-        st.k = 0;
-        st.cmin = INT_MAX;
-        st.cmax = -1;
-        st.rmin = 0;
-        st.rmax = 0;
     }
 }
 
-__global__ void big_clear_kernel(uint32_t *gkey, uint32_t *gcnt, int64_t nslots, const Ctl *ctl)
+// Empty the occupied slots of every big table (chunks of the occupied lists).
+__global__ void __launch_bounds__(kTB) big_clear_kernel(IterArgs p)
 {
-    if (!ctl_active(ctl)) return;
-    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nslots; s += (int64_t)gridDim.x * blockDim.x) {
-        gkey[s] = kEmpty;
-        gcnt[s] = 0;
+    if (!ctl_active(p.ctl)) return;
+    if ((int)blockIdx.x >= p.nschunks) return;
+    const int c = p.s0 + blockIdx.x;
+    const int bi = p.schunk_big[c];
+    const int d = p.bstat[bi].d;
+    const int64_t i0 = p.schunk_s0[c], i1 = min(p.schunk_s1[c], (int64_t)d);
+    const uint32_t *occ = p.big_occ + p.big_ooff[bi];
+    uint32_t *gk = p.gkey + p.big_toff[bi];
+    uint32_t *gc = p.gcnt + p.big_toff[bi];
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
+        const uint32_t sidx = occ[i];
+        gk[sidx] = kEmpty;
+        gc[sidx] = 0;
+    }
+}
+
+// Reset the per-big-vertex statistics for the next iteration.
+__global__ void big_reset_kernel(IterArgs p)
+{
+    if (!ctl_active(p.ctl)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.nbig; i += gridDim.x * blockDim.x) {
+        BigStat &b = p.bstat[p.b0 + i];
+        b.d = 0;
+        b.W = 0;
+        b.k = 0;
+        b.cmin = INT_MAX;
+        b.cmax = -1;
+        b.rmin = 0;
+        b.rmax = 0;
     }
 }
 
@@ -955,19 +1059,31 @@ __global__ void init_bigstat_kernel(BigStat *b, int nbig)
     }
 }
 
-// Input validation on the device: offsets non-decreasing, neighbours in [0, n).
-__global__ void validate_kernel(const int64_t *off, const int32_t *nbr, int64_t n, int64_t m, int *bad)
+// Input validation on the device: neighbours in [0, n).  (Offsets are checked on
+// the host before the schedule is built.)
+__global__ void validate_kernel(const int32_t *nbr, int64_t m, int64_t n, int *bad)
 {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int b = 0;
-    for (int64_t i = t0; i < n; i += stride)
-        if (off[i + 1] < off[i]) b |= 1;
-    for (int64_t e = t0; e < m; e += stride) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
         const int32_t x = nbr[e];
-        if (x < 0 || (int64_t)x >= n) b |= 2;
+        if (x < 0 || (int64_t)x >= n) b = 1;
     }
-    if (b) atomicOr(bad, b);
+    if (__any_sync(kFull, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+// Out-of-core: validate a streamed batch before its kernels run; a bad neighbour stops
+// the run (every later kernel returns at once) and is reported as a format error.
+__global__ void validate_batch_kernel(const int32_t *nbr, int64_t cnt, int64_t n, Ctl *ctl)
+{
+    int b = 0;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t x = nbr[e];
+        if (x < 0 || (int64_t)x >= n) b = 1;
+    }
+    if (__any_sync(kFull, b) && (threadIdx.x & 31) == 0) {
+        atomicOr(&ctl->err, kErrFormat);
+        atomicExch(&ctl->active, 0);
+    }
 }
 
 }  // namespace galp

@@ -2,7 +2,8 @@
 # Build oracle/_ref/ref_harness: the reference's own method-0 kernels
 # (label_propagation/src/dpp/kernel.cuh, src/common/segmented_reduce.cuh) and
 # host helpers (include/graph.h, src/common/outofcore.cuh), compiled from the
-# reference tree where it lies and run on the CPU through oracle/refsim/simt_shim.h.
+# reference tree where it lies and run on the CPU through oracle/refsim/simt_shim.h,
+# plus the reference's loaders (include/graph.h) and accuracy measures (include/accuracy.h).
 # Test infrastructure only.  Needs the reference tree (REF, default /root/reference);
 # exits 0 without building when it is absent.
 set -euo pipefail
@@ -16,7 +17,7 @@ fi
 mkdir -p "$HERE/_ref"
 # The kernels of segmented_reduce.cuh end where `struct SegmentedReducer` (host
 # launch code) begins; only that prefix is fed to the compiler, through a pipe.
-g++ -std=c++17 -O2 -w \
+g++ -std=c++17 -O2 -w -fopenmp \
     -include "$HERE/refsim/simt_shim.h" \
     -include <(sed '/^struct SegmentedReducer/,$d' "$LP/src/common/segmented_reduce.cuh") \
     -I "$HERE/refsim" -I "$LP/src" -I "$LP/include" \

@@ -24,11 +24,14 @@
 //      labels_out.bin: int32 labels after each executed iteration, concatenated
 //   ref_harness segreduce <TB> <ET> <in.bin> <out.bin>
 //      in.bin: int64 N, int64 M, int32 w[N], int32 seg_start[M]; out.bin: int32 sat[M]
+//   ref_harness csr <graph> <offsets_out.bin> <neighbors_out.bin>    CSRGraph loaders
+//   ref_harness acc <ground_truth> <labels.bin>                      compute_nmi/f_measure/ari
 // simt_shim.h and the kernel part of segmented_reduce.cuh (everything before
 // `struct SegmentedReducer`, whose host code uses <<<>>> launch syntax) are
 // force-included by oracle/build_ref.sh ahead of this file.
 #include "dpp/kernel.cuh"
 #include "graph.h"
+#include "accuracy.h"
 #include "common/outofcore.cuh"
 
 #include <fstream>
@@ -196,10 +199,36 @@ int run_segreduce(int TB, int ET, const char *in, const char *out)
     return 0;
 }
 
+int run_csr(const char *graph_file, const char *off_out, const char *nbr_out)
+{
+    CSRGraph<int32_t, int64_t> G(graph_file);
+    std::ofstream o(off_out, std::ios::binary);
+    o.write((const char *)G.offsets.data(), sizeof(int64_t) * G.offsets.size());
+    std::ofstream nb(nbr_out, std::ios::binary);
+    nb.write((const char *)G.neighbors.data(), sizeof(int32_t) * G.neighbors.size());
+    return 0;
+}
+
+int run_acc(const char *gt, const char *labels_file)
+{
+    std::ifstream f(labels_file, std::ios::binary | std::ios::ate);
+    const size_t n = (size_t)f.tellg() / sizeof(int);
+    f.seekg(0);
+    std::vector<int> labels(n);
+    f.read((char *)labels.data(), sizeof(int) * n);
+    const double nmi = compute_nmi(gt, labels);
+    const double fm = compute_f_measure(gt, labels);
+    const double ari = compute_ari(gt, labels);
+    std::printf("ACC %.17g %.17g %.17g\n", nmi, fm, ari);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv)
 {
+    if (argc >= 5 && std::string(argv[1]) == "csr") return run_csr(argv[2], argv[3], argv[4]);
+    if (argc >= 4 && std::string(argv[1]) == "acc") return run_acc(argv[2], argv[3]);
     if (argc >= 8 && std::string(argv[1]) == "lp")
         return run_lp(argv[2], atoi(argv[3]), atoi(argv[4]), atoi(argv[5]), argv[6], argv[7]);
     if (argc >= 6 && std::string(argv[1]) == "segreduce")
