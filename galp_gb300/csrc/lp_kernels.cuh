@@ -37,7 +37,6 @@ constexpr int kBigChunk = 4096;       // edges per big_insert CTA
 constexpr int kBigSlotChunk = 8192;   // table slots per big_stats CTA
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
-constexpr int kHardWarps = 4;         // warps of a tile CTA that resolve vertices needing full ranks
 constexpr long long kSpinLimit = 1ll << 20;  // look-back give-up bound (about a second)
 
 // error bits in Ctl::err
@@ -200,6 +199,77 @@ __device__ long long lookback_prefix(unsigned long long *status, long long t, un
     return P;
 }
 
+// Block-wide decoupled look-back: all kTB threads read kTB predecessors per round
+// trip, so a tile whose nearest published prefix lies a few hundred tiles back (the
+// usual case with hundreds of resident CTAs) waits for one or two L2 round trips.
+// Called by every thread of the block; returns the exclusive prefix to all.
+struct LookbackSmem {
+    long long wsum[kNW];
+    int wfirst[kNW];
+    long long P;
+    int done;
+};
+
+__device__ long long lookback_prefix_block(unsigned long long *status, long long t, unsigned epoch, long long D,
+                                           Ctl *ctl, LookbackSmem &L)
+{
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (t == 0) {
+        if (tid == 0) st_relaxed_u64(&status[0], pack_status(2, epoch, (unsigned long long)D));
+        return 0;
+    }
+    if (tid == 0) st_relaxed_u64(&status[t], pack_status(1, epoch, (unsigned long long)D));
+    const unsigned ep = epoch & kEpochMask;
+    long long P = 0;
+    long long j = t - 1;
+    for (;;) {
+        const long long jj = j - tid;
+        unsigned long long w = 0;
+        unsigned state = 2;
+        if (jj >= 0) {
+            long long spins = 0;
+            unsigned ns = 32;
+            for (;;) {
+                w = ld_relaxed_u64(&status[jj]);
+                state = (unsigned)(w >> kStateShift);
+                if (state != 0 && (unsigned)((w >> kEpochShift) & kEpochMask) == ep) break;
+                // give up after kSpinLimit polls, or at once when another wait already gave up
+                if (++spins > kSpinLimit || *((volatile int *)&ctl->err)) {
+                    atomicOr(&ctl->err, kErrLookback);
+                    state = 2;
+                    w = 0;
+                    break;
+                }
+                __nanosleep(ns);
+                if (ns < 1024) ns <<= 1;
+            }
+        } else {
+            w = 0;  // before the first tile: prefix 0
+        }
+        // nearest predecessor holding an inclusive prefix = smallest tid with state 2
+        const unsigned pm = __ballot_sync(kFull, state == 2);
+        if (lane == 0) L.wfirst[warp] = pm ? (warp * 32 + __ffs(pm) - 1) : INT_MAX;
+        __syncthreads();
+        int first = INT_MAX;
+#pragma unroll
+        for (int w2 = 0; w2 < kNW; ++w2) first = min(first, L.wfirst[w2]);
+        long long val = (tid <= first) ? (long long)(w & kValueMask) : 0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) val += __shfl_xor_sync(kFull, val, off);
+        if (lane == 0) L.wsum[warp] = val;
+        __syncthreads();
+        long long sum = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < kNW; ++w2) sum += L.wsum[w2];
+        P += sum;
+        __syncthreads();  // L is rewritten by the next round
+        if (first != INT_MAX) break;
+        j -= kTB;
+    }
+    if (tid == 0) st_relaxed_u64(&status[t], pack_status(2, epoch, (unsigned long long)(P + D)));
+    return P;
+}
+
 // ---------------------------------------------------------------------------
 // warp-level queries used for tied vertices that the per-vertex summary cannot decide
 // ---------------------------------------------------------------------------
@@ -223,6 +293,36 @@ struct WarpSmallQuery {
         const int key = __reduce_max_sync(kFull, in ? tile_priority(rk - lo) : -1);
         const unsigned m = __ballot_sync(kFull, in && tile_priority(rk - lo) == key);
         return m ? __shfl_sync(kFull, rk, __ffs(m) - 1) : -1;
+    }
+};
+
+// Sorted run list (labels ascending, counts) of a vertex of degree <= 32, scanned by
+// one thread.
+struct RunListQuery {
+    const uint32_t *lab;
+    const uint32_t *cnt;
+    int d, W;
+    __device__ int first_ge(int64_t x) const
+    {
+        for (int r = (int)(x < 0 ? 0 : x); r < d; ++r)
+            if ((int)cnt[r] == W) return r;
+        return -1;
+    }
+    __device__ int last_lt(int64_t y) const
+    {
+        for (int r = (int)(y < d ? y : d) - 1; r >= 0; --r)
+            if ((int)cnt[r] == W) return r;
+        return -1;
+    }
+    __device__ int tile_pick(int64_t lo) const
+    {
+        int best = -1, br = -1;
+        for (int r = 0; r < d; ++r)
+            if ((int)cnt[r] == W && r >= lo && r < lo + kTile && tile_priority(r - lo) > best) {
+                best = tile_priority(r - lo);
+                br = r;
+            }
+        return br;
     }
 };
 
@@ -413,8 +513,8 @@ struct TileSmem {
     int16_t vpref[kTileV];
     int16_t hard[kTileV];
     int16_t hard_rank[kTileV];
-    int32_t hist[kHardWarps][256];
     int32_t wtmp[kNW];
+    LookbackSmem lb;
     long long tile;
     long long P;
     long long N;
@@ -444,13 +544,11 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
 
         if (bi >= 0) {
             // single big vertex: its distinct count was computed by big_insert
-            if (warp == 0) {
-                const long long D = p.bstat[bi].d;
-                long long P = lookback_prefix(p.status, t, p.epoch, D, lane, p.ctl);
-                if (lane == 0) {
-                    p.big_a[bi] = P;
-                    if (v0 == p.last_v) p.ctl->N = P + D;
-                }
+            const long long D = *((volatile int *)&p.bstat[bi].d);
+            const long long P = lookback_prefix_block(p.status, t, p.epoch, D, p.ctl, S.lb);
+            if (tid == 0) {
+                p.big_a[bi] = P;
+                if (v0 == p.last_v) p.ctl->N = P + D;
             }
             __syncthreads();
             continue;
@@ -643,10 +741,42 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
                         const unsigned m = cm & vm;
                         cmin = cmax = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : lane);
                     } else {
-                        cmin = seg_min(cand ? lab : INT_MAX, lane, first, last);
-                        cmax = seg_max(cand ? lab : -1, lane, first, last);
-                        rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
-                        rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
+                        // Sort the pack by (vertex, label); vertices keep their lanes, equal
+                        // labels become adjacent runs in ascending order.  Each vertex's runs
+                        // (label, count) are written to its slots of hkey/hcnt (unused by
+                        // vertices of degree <= 32) for per-thread resolution later.
+                        unsigned long long sk = key;
+                        int sc = valid ? cnt : 0;
+#pragma unroll
+                        for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+                            for (int j = kk >> 1; j > 0; j >>= 1) {
+                                const unsigned long long ok = __shfl_xor_sync(kFull, sk, j);
+                                const int oc = __shfl_xor_sync(kFull, sc, j);
+                                const bool up = (lane & kk) == 0, lower = (lane & j) == 0;
+                                const bool take = (lower == up) ? (ok < sk) : (ok > sk);
+                                if (take) {
+                                    sk = ok;
+                                    sc = oc;
+                                }
+                            }
+                        }
+                        const int slab = (int)(unsigned)sk;
+                        const int prev = __shfl_up_sync(kFull, slab, 1);
+                        const bool head = valid && (lane == first || prev != slab);
+                        const unsigned hm = __ballot_sync(kFull, head) & vm;
+                        const int rank = __popc(hm & ((1u << lane) - 1));
+                        const unsigned cr = __ballot_sync(kFull, head && sc == W) & vm;
+                        if (head) {
+                            const int base = 2 * (int)S.vpos[v];
+                            S.hkey[base + rank] = (uint32_t)slab;
+                            S.hcnt[base + rank] = (uint32_t)sc;
+                        }
+                        const int lo = cr ? (__ffs(cr) - 1) : lane, hi = cr ? (31 - __clz(cr)) : lane;
+                        cmin = __shfl_sync(kFull, slab, lo);
+                        cmax = __shfl_sync(kFull, slab, hi);
+                        rmin = __popc(hm & ((1u << lo) - 1));
+                        rmax = __popc(hm & ((1u << hi) - 1));
                     }
                     if (valid && lane == first) {
                         S.vd[v] = d;
@@ -685,11 +815,11 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
             if (tid == 0) S.D = tot;
         }
         __syncthreads();
-        // P6: warp 0 obtains the tile's run base by look-back while the other warps
-        // write the vertices whose winner is unique (no position needed)
-        if (warp == 0) {
-            const long long P = lookback_prefix(p.status, t, p.epoch, S.D, lane, p.ctl);
-            if (lane == 0) {
+        // P6: the tile's run base by block-wide look-back, then the vertices whose
+        // winner is unique (no position needed)
+        {
+            const long long P = lookback_prefix_block(p.status, t, p.epoch, S.D, p.ctl, S.lb);
+            if (tid == 0) {
                 S.P = P;
                 if (p.last_v >= v0 && p.last_v < v1) {
                     S.N = P + S.D;
@@ -698,31 +828,37 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
                     S.N = -1;
                 }
             }
-        } else {
-            for (int i = tid - 32; i < nv; i += kTB - 32) {
-                const int v = v0 + i;
-                if (vdeg(S, i) == 0 || S.vk[i] == 1) {
-                    const int32_t old = __ldg(&p.lab_in[v]);
-                    const int32_t nl = vdeg(S, i) == 0 ? old : S.vcmin[i];
-                    p.lab_out[v] = nl;
-                    changes += (nl != old);
-                }
+        }
+        for (int i = tid; i < nv; i += kTB) {
+            const int v = v0 + i;
+            if (vdeg(S, i) == 0 || S.vk[i] == 1) {
+                const int32_t old = __ldg(&p.lab_in[v]);
+                const int32_t nl = vdeg(S, i) == 0 ? old : S.vcmin[i];
+                p.lab_out[v] = nl;
+                changes += (nl != old);
             }
         }
         __syncthreads();
-        // P7: resolve tied vertices from the summaries
+        // P7: resolve tied vertices: from the summary when it decides, from the sorted
+        // run list for vertices of degree <= 32, else by a warp query in P8
         for (int i = tid; i < nv; i += kTB) {
             if (vdeg(S, i) == 0 || S.vk[i] == 1) continue;
             const int v = v0 + i;
             const int32_t old = __ldg(&p.lab_in[v]);
             int32_t nl;
             const int k = S.vk[i], d = S.vd[i];
+            const long long a = S.P + S.vpref[i];
             SummaryQuery q(k, d, S.vrmin[i], S.vrmax[i]);
-            const int r = resolve_rank(S.P + S.vpref[i], d, S.N, v == p.last_v, q);
+            int r = resolve_rank(a, d, S.N, v == p.last_v, q);
             if (!q.fail && r == S.vrmin[i]) {
                 nl = S.vcmin[i];
             } else if (!q.fail && r == S.vrmax[i]) {
                 nl = S.vcmax[i];
+            } else if (vdeg(S, i) <= kSmallMax) {
+                const int base = 2 * (int)S.vpos[i];
+                RunListQuery rq{&S.hkey[base], &S.hcnt[base], d, S.vW[i]};
+                if (q.fail) r = resolve_rank(a, d, S.N, v == p.last_v, rq);
+                nl = (int32_t)S.hkey[base + r];
             } else {
                 const int h = atomicAdd(&S.nhard, 1);
                 S.hard[h] = (int16_t)i;
@@ -733,41 +869,23 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
             changes += (nl != old);
         }
         __syncthreads();
-        // P8: tied vertices that need the full candidate ranks
+        // P8: tied vertices above 32 edges whose summary does not decide: warp queries
+        // over the vertex's hash region (radix-select histograms alias the label slots,
+        // which are no longer needed)
         if (S.nhard) {
-            for (int h = warp; warp < kHardWarps && h < S.nhard; h += kHardWarps) {
+            int *hist = reinterpret_cast<int *>(S.lab) + warp * 256;
+            for (int h = warp; h < S.nhard; h += kNW) {
                 const int i = S.hard[h];
                 int r = S.hard_rank[h];
                 const int v = v0 + i;
                 const int deg = vdeg(S, i);
                 const int d = S.vd[i], W = S.vW[i];
                 const long long a = S.P + S.vpref[i];
-                const bool is_last = v == p.last_v;
-                int32_t label;
-                if (deg <= kSmallMax) {
-                    const int pos = S.vpos[i];
-                    const bool valid = lane < deg;
-                    const int lab = valid ? S.lab[pos + lane] : 0;
-                    const unsigned key = valid ? (unsigned)lab : (0x80000000u | (unsigned)lane);
-                    const unsigned eq = __match_any_sync(kFull, key);
-                    const int cnt = __popc(eq);
-                    const bool leader = valid && ((__ffs(eq) - 1) == lane);
-                    int rk = 0;
-                    for (int j = 0; j < deg; ++j) {
-                        const int lj = __shfl_sync(kFull, lab, j);
-                        const bool ldj = __shfl_sync(kFull, leader, j);
-                        rk += (ldj && lj < lab);
-                    }
-                    WarpSmallQuery q{leader && cnt == W, rk};
-                    if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
-                    const unsigned m = __ballot_sync(kFull, leader && rk == r);
-                    label = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : 0);
-                } else {
-                    WarpTableQuery q{&S.hkey[2 * S.vpos[i]], &S.hcnt[2 * S.vpos[i]], 2 * pad32(deg), d, W,
-                                     S.vrmin[i], S.vrmax[i], S.hist[warp], lane, nullptr};
-                    if (r < 0) r = resolve_rank(a, d, S.N, is_last, q);
-                    label = (r == S.vrmin[i]) ? S.vcmin[i] : (r == S.vrmax[i]) ? S.vcmax[i] : (int32_t)q.select(r);
-                }
+                WarpTableQuery q{&S.hkey[2 * S.vpos[i]], &S.hcnt[2 * S.vpos[i]], 2 * pad32(deg), d, W,
+                                 S.vrmin[i], S.vrmax[i], hist, lane, nullptr};
+                if (r < 0) r = resolve_rank(a, d, S.N, v == p.last_v, q);
+                const int32_t label =
+                    (r == S.vrmin[i]) ? S.vcmin[i] : (r == S.vrmax[i]) ? S.vcmax[i] : (int32_t)q.select(r);
                 if (lane == 0) {
                     const int32_t old = __ldg(&p.lab_in[v]);
                     p.lab_out[v] = label;
@@ -805,16 +923,31 @@ __global__ void __launch_bounds__(kTB) big_insert_kernel(IterArgs p)
         scnt[s] = 0;
     }
     __syncthreads();
-    for (int64_t e = e0 + threadIdx.x; e < e1; e += kTB) {
-        const uint32_t L = (uint32_t)__ldg(&p.lab_in[__ldg(&p.nbr[e])]);
-        uint32_t h = hslot(L, cap);
-        for (;;) {
-            uint32_t prev = atomicCAS(&skey[h], kEmpty, L);
-            if (prev == kEmpty || prev == L) {
-                atomicAdd(&scnt[h], 1u);
-                break;
+    {
+        // all of a thread's neighbour loads, then all its label gathers, in flight together
+        constexpr int PER = kBigChunk / kTB;
+        int nb[PER];
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const int64_t e = e0 + threadIdx.x + (int64_t)i * kTB;
+            nb[i] = (e < e1) ? __ldg(&p.nbr[e]) : -1;
+        }
+        uint32_t lb[PER];
+#pragma unroll
+        for (int i = 0; i < PER; ++i) lb[i] = (nb[i] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[i]]) : kEmpty;
+#pragma unroll
+        for (int i = 0; i < PER; ++i) {
+            const uint32_t L = lb[i];
+            if (L == kEmpty) continue;
+            uint32_t h = hslot(L, cap);
+            for (;;) {
+                uint32_t prev = atomicCAS(&skey[h], kEmpty, L);
+                if (prev == kEmpty || prev == L) {
+                    atomicAdd(&scnt[h], 1u);
+                    break;
+                }
+                h = (h + 1 == cap) ? 0 : h + 1;
             }
-            h = (h + 1 == cap) ? 0 : h + 1;
         }
     }
     __syncthreads();
@@ -825,29 +958,36 @@ __global__ void __launch_bounds__(kTB) big_insert_kernel(IterArgs p)
     uint32_t *occ = p.big_occ + p.big_ooff[bi];
     int *dcount = &p.bstat[bi].d;
     const int lane = threadIdx.x & 31;
-    for (int s = threadIdx.x; s < (int)cap; s += kTB) {  // cap is a multiple of kTB
-        const uint32_t L = skey[s];
-        bool created = false;
-        uint32_t h = 0;
-        if (L != kEmpty) {
-            h = hslot(L, gcap);
-            for (;;) {
-                uint32_t prev = atomicCAS(&gk[h], kEmpty, L);
-                if (prev == kEmpty || prev == L) {
-                    created = prev == kEmpty;
-                    atomicAdd(&gc[h], scnt[s]);
-                    break;
-                }
-                h = (h + 1 == gcap) ? 0 : h + 1;
-            }
+    constexpr int U = 8;  // slots per thread with their table CAS in flight together
+    for (int base = 0; base < (int)cap; base += kTB * U) {  // cap is a multiple of kTB * U
+        uint32_t L[U], h[U], prev[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            L[u] = skey[base + u * kTB + threadIdx.x];
+            h[u] = (L[u] != kEmpty) ? hslot(L[u], gcap) : 0;
         }
-        // record newly occupied slots in the vertex's occupied list (warp-aggregated)
-        const unsigned m = __ballot_sync(kFull, created);
-        if (m) {
-            int base = 0;
-            if (lane == __ffs(m) - 1) base = atomicAdd(dcount, __popc(m));
-            base = __shfl_sync(kFull, base, __ffs(m) - 1);
-            if (created) occ[base + __popc(m & ((1u << lane) - 1))] = h;
+#pragma unroll
+        for (int u = 0; u < U; ++u) prev[u] = (L[u] != kEmpty) ? atomicCAS(&gk[h[u]], kEmpty, L[u]) : kEmpty;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            bool created = false;
+            if (L[u] != kEmpty) {
+                // linear probing past slots owned by other labels (rare at load <= 1/2)
+                while (prev[u] != kEmpty && prev[u] != L[u]) {
+                    h[u] = (h[u] + 1 == gcap) ? 0 : h[u] + 1;
+                    prev[u] = atomicCAS(&gk[h[u]], kEmpty, L[u]);
+                }
+                created = prev[u] == kEmpty;
+                atomicAdd(&gc[h[u]], scnt[base + u * kTB + threadIdx.x]);
+            }
+            // record newly occupied slots in the vertex's occupied list (warp-aggregated)
+            const unsigned m = __ballot_sync(kFull, created);
+            if (m) {
+                int ob = 0;
+                if (lane == __ffs(m) - 1) ob = atomicAdd(dcount, __popc(m));
+                ob = __shfl_sync(kFull, ob, __ffs(m) - 1);
+                if (created) occ[ob + __popc(m & ((1u << lane) - 1))] = h[u];
+            }
         }
     }
 }
