@@ -29,7 +29,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CUDA_SOURCES = ["galp_capi.cu", "galp_tools.cu"]
+CUDA_SOURCES = ["galp_capi.cu", "galp_tools.cu", "galp_noalloc.cu"]
 HOST_SOURCES = ["host/graph_io.cpp", "host/accuracy.cpp"]
 
 

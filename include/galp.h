@@ -108,6 +108,25 @@ int galp_enqueue(galp_ctx *ctx, int32_t niter);
 /* Wait for enqueued work and fill stats (iterations, counts, errors). */
 int galp_sync(galp_ctx *ctx, galp_stats *stats);
 
+/* Label propagation without device allocation, for callers that cannot call
+ * cudaMalloc (a host framework or external allocator owns all device memory, or an
+ * allocation's synchronisation is not acceptable on the calling path).  No
+ * counterpart in the reference.  Same update and labels as galp_create + galp_run +
+ * galp_get_labels with method 0, policy 0, but every device buffer lives in one
+ * static device array of 12.5 MiB that each GPU loading the library holds until the
+ * process exits; nothing is allocated on the device or the host.
+ *   graph       host CSR; at most GALP_NOALLOC_MAX_VERTICES vertices, at most
+ *               GALP_NOALLOC_MAX_ENTRIES entries, no vertex above 2048 neighbours
+ *               (GALP_EUNSUPPORTED otherwise)
+ *   labels_out  host int32[n]; stats may be NULL; stream: cudaStream_t or NULL
+ * The first call on a device (with that device current) sets up the array's address
+ * and should come before any stream capture.  Calls on a device share the array;
+ * calls that overlap on the GPU race on it (calls from one process are serialised). */
+#define GALP_NOALLOC_MAX_VERTICES (1 << 17)
+#define GALP_NOALLOC_MAX_ENTRIES (1 << 21)
+int galp_run_noalloc(const galp_csr *graph, int32_t niter, int32_t early_exit, int32_t *labels_out,
+                     galp_stats *stats, void *stream);
+
 /* Host-side evaluation of the tie-break closed form, for tests: winning candidate
  * rank of a vertex with run base a, distinct count d, in a scope of N runs, given
  * its candidate ranks cand[k] (ascending). */
