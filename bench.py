@@ -305,14 +305,14 @@ def run_gpu(args, g, desc, rank, world, dist):
     n, m, mb = info.n, info.m, info.m_big
     # algorithmic bytes: 4 B neighbour + 4 B gathered label per CSR entry, 8 B offset,
     # 4 B old + 4 B new label per vertex (8m + 16n + 8 per dense iteration)
-    tile_bytes = 8 * (m - mb) + 16 * n + 8
+    pipe_bytes = 8 * (m - mb) + 16 * n + 8
     big_bytes = 8 * mb
-    shares = {"lp_tile_kernel": kt.tile_ms, "big_vertex_kernels": kt.big_pre_ms + kt.big_post_ms}
+    shares = {"count_scan_resolve": kt.pipe_ms, "big_vertex_kernels": kt.big_pre_ms + kt.big_post_ms}
     dom = max(shares, key=shares.get)
-    if dom == "lp_tile_kernel":
-        launches = max(kt.tile_launches, 1)
-        dur = kt.tile_ms / launches
-        alg = tile_bytes
+    if dom == "count_scan_resolve":
+        launches = max(kt.pipe_groups, 1)
+        dur = kt.pipe_ms / launches
+        alg = pipe_bytes
     else:
         launches = max(kt.big_pre_groups, 1)
         dur = (kt.big_pre_ms + kt.big_post_ms) / launches
@@ -360,8 +360,9 @@ def run_gpu(args, g, desc, rank, world, dist):
     cfg = dict(desc)
     cfg.update(iterations_per_step=NITER, early_exit=False, method=0, policy=0,
                l2="inputs larger than L2 (neighbours {:.1f} GB vs 129 MB L2)".format(4 * g.m / 1e9),
-               parallelism="replicas" if world > 1 else "single-gpu", ntiles=int(info.ntiles),
-               big_vertices=int(info.nbig), big_edges=int(info.m_big))
+               parallelism="replicas" if world > 1 else "single-gpu", packs=int(info.npacks),
+               mid_vertices=int(info.nmid), large_vertices=int(info.nlarge), big_vertices=int(info.nbig),
+               big_edges=int(info.m_big))
     line = {
         "metric": "GTEPS per LP iteration", "value": round(value, 3), "unit": "GTEPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),

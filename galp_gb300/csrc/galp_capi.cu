@@ -1,12 +1,12 @@
 // galp_capi.cu -- host side of the C ABI (include/galp.h): context, schedule, launches.
 //
 // In-core (policy 0) keeps the whole CSR resident in HBM: neighbours int32[m],
-// offsets int64[n+1] (no int32 truncation, unlike src/common/incore.cuh:63-69),
-// two label buffers, and a static schedule built once per graph:
-//   vpos[n]      uint16 slot of each vertex inside its tile
-//   tile_v0[T+1] first vertex of each tile, tile_used[T] slots used,
-//   tile_big[T]  big-vertex index for single-vertex tiles of degree > kTileSlots
-// plus open-addressed global tables for the big vertices.
+// offsets int64[n+1] (no int32 truncation, unlike src/common/incore.cuh:63-69), two
+// label buffers, per-vertex count/scan state, a spill area for tied vertices' runs,
+// and a static degree-bucketed schedule built once per graph (packs of small
+// vertices, mid/large vertex lists, big vertices with open-addressed global tables).
+// Out-of-core (policies 1/2) keeps everything but the neighbours resident and streams
+// the neighbours of one batch at a time.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,48 +50,59 @@ int cuda_status(cudaError_t e)
         if (e_ != cudaSuccess) return cuda_status(e_);     \
     } while (0)
 
-// Static per-graph schedule (host).  Within every scope, consecutive vertices are
-// packed into tiles whose labels fit kTileSlots shared-memory slots (at most kTileV
-// vertices): a vertex of degree <= 32 never straddles a 32-slot pack, larger ones
-// start on a pack boundary, and vertices above kTileSlots become single-vertex big
-// tiles with a global hash table (offsets relative to the scope, so out-of-core
-// batches reuse one table area).
+// Static per-graph schedule (host), per scope: packs of consecutive vertices of
+// degree <= 32 (at most 32 vertices and 32 edges; a pack ends at a vertex of another
+// bucket), mid (33..256) and large (257..2048) vertex lists, and big vertices (> 2048)
+// with global hash tables (offsets relative to the scope, so out-of-core batches reuse
+// one table area) and their work chunks.
 void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts)
 {
     S = Schedule();
-    S.vpos.assign((size_t)n, 0);
+    std::vector<int32_t> large, xl;
     for (size_t k = 0; k + 1 < scope_starts.size(); ++k) {
         Scope sc;
         sc.v0 = scope_starts[k];
         sc.v1 = scope_starts[k + 1];
         sc.e0 = off[sc.v0];
         sc.e1 = off[sc.v1];
-        sc.t0 = (int32_t)S.tile_big.size();
+        sc.p0 = (int32_t)S.pack_v0.size();
+        sc.m0 = (int32_t)S.mid_v.size();
         sc.b0 = (int32_t)S.big_v.size();
         sc.c0 = (int32_t)S.chunk_big.size();
         sc.s0 = (int32_t)S.schunk_big.size();
-        int cur = 0, nvt = 0;
-        int64_t tstart = sc.v0;
-        auto close = [&](int64_t vend) {
-            if (vend > tstart) {
-                S.tile_v0.push_back((int32_t)tstart);
-                S.tile_big.push_back(-1);
-                S.tile_used.push_back((uint16_t)cur);
+        large.clear();
+        xl.clear();
+        int pv = 0, pe = 0;  // vertices / edges in the open pack
+        int64_t pstart = -1;
+        auto close = [&]() {
+            if (pv) {
+                S.pack_v0.push_back((int32_t)pstart);
+                S.pack_nv.push_back((uint8_t)pv);
             }
-            tstart = vend;
-            cur = 0;
-            nvt = 0;
+            pv = pe = 0;
+            pstart = -1;
         };
-        int64_t toff = 0, ooff = 0;
+        int64_t toff = 0, ooff = 0, nsmall = 0;
         for (int64_t v = sc.v0; v < sc.v1; ++v) {
             const int64_t deg = off[v + 1] - off[v];
             if (deg > 0) sc.last_v = (int32_t)v;
-            if (deg > kTileSlots) {
-                close(v);
+            if (deg <= kSmallMax) {
+                if (pv == 32 || pe + deg > 32) close();
+                if (!pv) pstart = v;
+                pv++;
+                pe += (int)deg;
+                nsmall++;
+                continue;
+            }
+            close();
+            if (deg <= kMidSMax) {
+                S.mid_v.push_back((int32_t)v);
+            } else if (deg <= kLargeMax) {
+                large.push_back((int32_t)v);
+            } else if (deg <= kXlMax) {
+                xl.push_back((int32_t)v);
+            } else {  // big: global table
                 const int32_t b = (int32_t)S.big_v.size();
-                S.tile_v0.push_back((int32_t)v);
-                S.tile_big.push_back(b);
-                S.tile_used.push_back(0);
                 S.big_v.push_back((int32_t)v);
                 uint32_t cap = 1;
                 while ((int64_t)cap < 2 * deg) cap <<= 1;
@@ -111,33 +122,15 @@ void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
                 toff += cap;
                 ooff += deg;
                 S.m_big += deg;
-                tstart = v + 1;
-                continue;
             }
-            auto place = [&](int c, int &pos, int &end) {
-                if (deg == 0) {
-                    pos = c;
-                    end = c;
-                } else if (deg <= kSmallMax) {
-                    pos = ((c & 31) + (int)deg > 32) ? ((c + 31) & ~31) : c;
-                    end = pos + (int)deg;
-                } else {
-                    pos = (c + 31) & ~31;
-                    end = pos + (((int)deg + 31) & ~31);
-                }
-            };
-            int pos, end;
-            place(cur, pos, end);
-            if (nvt == kTileV || end > kTileSlots) {
-                close(v);
-                place(0, pos, end);
-            }
-            S.vpos[(size_t)v] = (uint16_t)pos;
-            cur = end;
-            nvt++;
         }
-        close(sc.v1);
-        sc.nt = (int32_t)S.tile_big.size() - sc.t0;
+        close();
+        sc.nms = (int32_t)S.mid_v.size() - sc.m0;
+        S.mid_v.insert(S.mid_v.end(), large.begin(), large.end());
+        sc.nml = (int32_t)large.size();
+        S.mid_v.insert(S.mid_v.end(), xl.begin(), xl.end());
+        sc.nmx = (int32_t)xl.size();
+        sc.np = (int32_t)S.pack_v0.size() - sc.p0;
         sc.nb = (int32_t)S.big_v.size() - sc.b0;
         sc.nc = (int32_t)S.chunk_big.size() - sc.c0;
         sc.ns = (int32_t)S.schunk_big.size() - sc.s0;
@@ -146,9 +139,11 @@ void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         S.max_table_slots = std::max(S.max_table_slots, toff);
         S.max_occ_slots = std::max(S.max_occ_slots, ooff);
         S.max_scope_edges = std::max(S.max_scope_edges, sc.e1 - sc.e0);
+        S.max_scope_small = std::max(S.max_scope_small, nsmall);
+        S.max_scope_mid = std::max<int64_t>(S.max_scope_mid, (int64_t)sc.nms + sc.nml + sc.nmx);
+        S.max_scope_vertices = std::max(S.max_scope_vertices, sc.v1 - sc.v0);
         S.scopes.push_back(sc);
     }
-    S.tile_v0.push_back((int32_t)n);
 }
 
 int batch_boundaries(int64_t n, const int64_t *off, int buffer_pow, std::vector<int64_t> &bbs)
@@ -201,6 +196,7 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     m = g.m;
     policy = o.policy;
     h_nbr = g.neighbors;
+    frontier = o.frontier != 0 && policy == 0;  // the frontier needs the whole graph resident
     for (int64_t v = 0; v < n; ++v)
         if (g.offsets[v + 1] < g.offsets[v]) return GALP_EFORMAT;
     std::vector<int64_t> starts;
@@ -237,10 +233,9 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
         }
     }
     int rc;
-    if ((rc = upload(b_vpos, d_vpos, sched.vpos, st, h2d))) return rc;
-    if ((rc = upload(b_tile_v0, d_tile_v0, sched.tile_v0, st, h2d))) return rc;
-    if ((rc = upload(b_tile_big, d_tile_big, sched.tile_big, st, h2d))) return rc;
-    if ((rc = upload(b_tile_used, d_tile_used, sched.tile_used, st, h2d))) return rc;
+    if ((rc = upload(b_pack_v0, d_pack_v0, sched.pack_v0, st, h2d))) return rc;
+    if ((rc = upload(b_pack_nv, d_pack_nv, sched.pack_nv, st, h2d))) return rc;
+    if ((rc = upload(b_mid_v, d_mid_v, sched.mid_v, st, h2d))) return rc;
     if ((rc = upload(b_big_v, d_big_v, sched.big_v, st, h2d))) return rc;
     if ((rc = upload(b_big_toff, d_big_toff, sched.big_toff, st, h2d))) return rc;
     if ((rc = upload(b_big_tcap, d_big_tcap, sched.big_tcap, st, h2d))) return rc;
@@ -251,12 +246,26 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     if ((rc = upload(b_schunk_big, d_schunk_big, sched.schunk_big, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s0, d_schunk_s0, sched.schunk_s0, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s1, d_schunk_s1, sched.schunk_s1, st, h2d))) return rc;
+    // per-vertex state, spill and tied lists
+    const size_t nn = (size_t)std::max<int64_t>(n, 1);
+    GALP_CUDA(b_dcnt.alloc(sizeof(int32_t) * nn));
+    GALP_CUDA(b_runbase.alloc(sizeof(int64_t) * nn));
+    GALP_CUDA(b_c0.alloc(sizeof(int32_t) * nn));
+    GALP_CUDA(b_c1.alloc(sizeof(int32_t) * nn));
+    GALP_CUDA(b_kw.alloc(sizeof(int32_t) * nn));
+    GALP_CUDA(b_r.alloc(sizeof(int32_t) * nn));
+    const size_t ms = (size_t)std::max<int64_t>(sched.max_scope_edges, 1);
+    GALP_CUDA(b_run_lab.alloc(sizeof(int32_t) * ms));
+    GALP_CUDA(b_run_cnt.alloc(sizeof(uint16_t) * ms));
+    GALP_CUDA(b_tsmall.alloc(sizeof(int32_t) * (size_t)std::max<int64_t>(sched.max_scope_small, 1)));
+    GALP_CUDA(b_tmid.alloc(sizeof(int32_t) * (size_t)std::max<int64_t>(sched.max_scope_mid, 1)));
+    GALP_CUDA(b_bsum.alloc(sizeof(int64_t) * (size_t)std::max<int64_t>((sched.max_scope_vertices + kScanBlock - 1) / kScanBlock, 1)));
+    if (frontier) {
+        GALP_CUDA(b_dirty.alloc(nn));
+        GALP_CUDA(b_changed.alloc(sizeof(int32_t) * nn));
+    }
     GALP_CUDA(b_lab0.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
     GALP_CUDA(b_lab1.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
-    int32_t max_nt = 1;
-    for (const Scope &sc : sched.scopes) max_nt = std::max(max_nt, sc.nt);
-    GALP_CUDA(b_status.alloc(sizeof(unsigned long long) * max_nt));
-    GALP_CUDA(cudaMemsetAsync(b_status.p, 0, sizeof(unsigned long long) * max_nt, st));
     GALP_CUDA(b_ctl.alloc(sizeof(Ctl)));
     const size_t nbig = sched.big_v.size();
     GALP_CUDA(b_bstat.alloc(sizeof(BigStat) * std::max<size_t>(nbig, 1)));
@@ -282,31 +291,31 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
         GALP_CUDA(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         GALP_CUDA(cudaStreamSynchronize(st));
         if (bad) return GALP_EFORMAT;
+        // strictly increasing adjacency enables the first-iteration shortcut
+        GALP_CUDA(cudaMemsetAsync(b_bad.p, 0, sizeof(int), st));
+        adjacency_order_kernel<<<1024, 256, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p, n,
+                                                     (int *)b_bad.p);
+        GALP_CUDA(cudaGetLastError());
+        int unsorted = 0;
+        GALP_CUDA(cudaMemcpyAsync(&unsorted, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GALP_CUDA(cudaStreamSynchronize(st));
+        adj_sorted = unsorted == 0;
     }
     GALP_CUDA(cudaStreamSynchronize(st));
 
-    int dev = 0, sms = 0;
+    int dev = 0;
     GALP_CUDA(cudaGetDevice(&dev));
     GALP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    GALP_CUDA(cudaFuncSetAttribute(lp_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem)));
-    int occ = 0;
-    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lp_tile_kernel, kTB, sizeof(TileSmem)));
-    tile_grid = std::max(occ, 1) * sms;
+    GALP_CUDA(cudaFuncSetAttribute(count_cta_kernel<512, kXlSlots>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(uint32_t) * 2 * kXlSlots)));
     return GALP_OK;
 }
 
-IterArgs Engine::args(const Scope &sc) const
+IterArgs Engine::big_args(const Scope &sc) const
 {
     IterArgs a{};
     a.off = (const int64_t *)b_off.p;
-    a.vpos = d_vpos;
-    a.tile_v0 = d_tile_v0;
-    a.tile_big = d_tile_big;
-    a.tile_used = d_tile_used;
-    a.t0 = sc.t0;
-    a.ntiles = sc.nt;
     a.last_v = sc.last_v;
-    a.status = (unsigned long long *)b_status.p;
     a.ctl = (Ctl *)b_ctl.p;
     a.b0 = sc.b0;
     a.nbig = sc.nb;
@@ -329,37 +338,94 @@ IterArgs Engine::args(const Scope &sc) const
     a.bstat = (BigStat *)b_bstat.p;
     a.big_a = (int64_t *)b_big_a.p;
     a.big_occ = (uint32_t *)b_occ.p;
+    a.runbase = (const int64_t *)b_runbase.p;
     a.nbr_shift = (policy == 0) ? 0 : sc.e0;
     return a;
 }
 
+PipeArgs Engine::pipe_args(const Scope &sc) const
+{
+    PipeArgs q{};
+    q.nbr_shift = (policy == 0) ? 0 : sc.e0;
+    q.off = (const int64_t *)b_off.p;
+    q.ctl = (Ctl *)b_ctl.p;
+    q.pack_v0 = d_pack_v0 + sc.p0;
+    q.pack_nv = d_pack_nv + sc.p0;
+    q.npacks = sc.np;
+    q.mid_v = d_mid_v + sc.m0;
+    q.nmid_s = sc.nms;
+    q.nmid_l = sc.nml;
+    q.nmid_x = sc.nmx;
+    q.dcnt = (int32_t *)b_dcnt.p;
+    q.runbase = (int64_t *)b_runbase.p;
+    q.sm_c0 = (int32_t *)b_c0.p;
+    q.sm_c1 = (int32_t *)b_c1.p;
+    q.sm_kw = (int32_t *)b_kw.p;
+    q.sm_r = (int32_t *)b_r.p;
+    q.run_lab = (int32_t *)b_run_lab.p;
+    q.run_cnt = (uint16_t *)b_run_cnt.p;
+    q.tied_small = (int32_t *)b_tsmall.p;
+    q.tied_mid = (int32_t *)b_tmid.p;
+    q.v0 = sc.v0;
+    q.v1 = sc.v1;
+    q.bsum = (int64_t *)b_bsum.p;
+    q.last_v = sc.last_v;
+    return q;
+}
+
 // One update of one scope: reads lab_in (all vertices), writes lab_out for the scope.
 int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
-                          int32_t *lab_out)
+                          int32_t *lab_out, const uint8_t *dirty, int32_t *changed)
 {
-    IterArgs a = args(sc);
+    IterArgs a = big_args(sc);
     a.nbr = nbr;
     a.lab_in = lab_in;
     a.lab_out = lab_out;
-    if (++epoch > (unsigned)kEpochMask) {
-        epoch = 1;
-        GALP_CUDA(cudaMemsetAsync(b_status.p, 0, b_status.bytes, st));
-    }
-    a.epoch = epoch;
-    GALP_CUDA(cudaMemsetAsync(&((Ctl *)b_ctl.p)->ticket, 0, sizeof(unsigned long long), st));
+    a.changed = changed;
+    PipeArgs q = pipe_args(sc);
+    q.nbr = nbr;
+    q.lab_in = lab_in;
+    q.lab_out = lab_out;
+    q.dirty = dirty;
+    q.changed = changed;
+    Ctl *ctl = (Ctl *)b_ctl.p;
+    GALP_CUDA(cudaMemsetAsync(&ctl->tied_small, 0, 2 * sizeof(int), st));
     int e0 = -1;
     if (a.nbig) {
         if (prof.on) e0 = prof.mark(st);
         big_insert_kernel<<<a.nchunks, kTB, 0, st>>>(a);
         for (int pass = 0; pass < 3; ++pass) big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a, pass);
+        big_dcnt_kernel<<<(a.nbig + 255) / 256, 256, 0, st>>>(a, q.dcnt);
         if (prof.on) prof.spans[1].push_back({e0, prof.mark(st)});
     }
-    if (a.ntiles) {
-        if (prof.on) e0 = prof.mark(st);
-        const int grid = std::min<int>(tile_grid, a.ntiles);
-        lp_tile_kernel<<<grid, kTB, sizeof(TileSmem), st>>>(a);
-        if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
+    if (prof.on) e0 = prof.mark(st);
+    if (q.npacks) {
+        const int blocks = (int)std::min<int64_t>(((int64_t)q.npacks * 32 + 255) / 256, (int64_t)sms * 16);
+        count_small_kernel<<<blocks, 256, 0, st>>>(q);
     }
+    if (q.nmid_s) {
+        const int blocks = (int)std::min<int64_t>((q.nmid_s + kMidWarps - 1) / kMidWarps, (int64_t)sms * 6);
+        count_mid_kernel<<<blocks, 32 * kMidWarps, 0, st>>>(q);
+    }
+    if (q.nmid_l) {
+        const int blocks = (int)std::min<int64_t>(q.nmid_l, (int64_t)sms * 6);
+        count_cta_kernel<kTB, 2 * kLargeMax><<<blocks, kTB, sizeof(uint32_t) * 4 * kLargeMax, st>>>(q, q.nmid_s, q.nmid_l);
+    }
+    if (q.nmid_x) {
+        const int blocks = (int)std::min<int64_t>(q.nmid_x, (int64_t)sms);
+        count_cta_kernel<512, kXlSlots><<<blocks, 512, sizeof(uint32_t) * 2 * kXlSlots, st>>>(q, q.nmid_s + q.nmid_l,
+                                                                                            q.nmid_x);
+    }
+    const int64_t nv = sc.v1 - sc.v0;
+    if (nv > 0) {
+        const int nblk = (int)((nv + kScanBlock - 1) / kScanBlock);
+        scan_reduce_kernel<<<nblk, kTB, 0, st>>>(q);
+        scan_spine_kernel<<<1, kTB, 0, st>>>(q, nblk);
+        scan_apply_kernel<<<nblk, kTB, 0, st>>>(q);
+    }
+    resolve_small_kernel<<<sms * 4, kTB, 0, st>>>(q);
+    if (q.nmid_s + q.nmid_l + q.nmid_x) resolve_mid_kernel<<<sms * 2, kTB, 0, st>>>(q);
+    if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
     if (a.nbig) {
         if (prof.on) e0 = prof.mark(st);
         big_resolve_kernel<<<a.nbig, 32, sizeof(uint32_t) * kPickScratch, st>>>(a);
@@ -387,10 +453,39 @@ int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
     int32_t *lab[2] = {(int32_t *)b_lab0.p, (int32_t *)b_lab1.p};
     int rc = enqueue_init(st, niter, thr);
     if (rc) return rc;
+    Ctl *ctl = (Ctl *)b_ctl.p;
+    uint8_t *dirty = frontier ? (uint8_t *)b_dirty.p : nullptr;
+    int32_t *changed = frontier ? (int32_t *)b_changed.p : nullptr;
+    bool full_state = false;  // per-vertex counts and summaries hold the previous iteration
     for (int it = 0; it < niter; ++it) {
-        if ((rc = enqueue_scope(st, sched.scopes[0], (const int32_t *)b_nbr[0].p, lab[it & 1], lab[(it + 1) & 1])))
-            return rc;
-        finalize_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p);
+        const uint8_t *dirty_it = nullptr;
+        if (frontier) {
+            if (full_state) {
+                // vertices next to a label that changed in the previous iteration
+                GALP_CUDA(cudaMemsetAsync(dirty, 0, (size_t)n, st));
+                mark_dirty_kernel<<<sms * 8, kTB, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p,
+                                                           changed, (int)n, ctl, dirty);
+                dirty_it = dirty;
+            }
+            GALP_CUDA(cudaMemsetAsync(&ctl->changed_n, 0, sizeof(int), st));
+        }
+        if (it == 0 && adj_sorted && n > 0) {
+            PipeArgs q = pipe_args(sched.scopes[0]);
+            q.nbr = (const int32_t *)b_nbr[0].p;
+            q.lab_in = lab[0];
+            q.lab_out = lab[1];
+            q.changed = changed;
+            int e0 = prof.on ? prof.mark(st) : -1;
+            first_iteration_kernel<<<(int)std::min<int64_t>((n + kTB - 1) / kTB, (int64_t)sms * 8), kTB, 0, st>>>(q, n, m);
+            if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
+            full_state = false;  // the shortcut leaves no per-vertex counts behind
+        } else {
+            if ((rc = enqueue_scope(st, sched.scopes[0], (const int32_t *)b_nbr[0].p, lab[it & 1], lab[(it + 1) & 1],
+                                    dirty_it, changed)))
+                return rc;
+            full_state = true;
+        }
+        finalize_kernel<<<1, 1, 0, st>>>(ctl);
     }
     GALP_CUDA(cudaGetLastError());
     return GALP_OK;
@@ -643,10 +738,17 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
     info->n = ctx->n;
     info->m = ctx->m;
     info->m_big = E.sched.m_big;
-    info->ntiles = (int64_t)E.sched.tile_big.size();
+    info->npacks = (int64_t)E.sched.pack_v0.size();
+    int64_t nms = 0, nml = 0;
+    for (const galp::Scope &sc : E.sched.scopes) {
+        nms += sc.nms;
+        nml += sc.nml;
+    }
+    info->nmid = nms;
+    info->nlarge = nml;
     info->nbig = (int64_t)E.sched.big_v.size();
     info->table_slots = E.sched.max_table_slots;
-    info->launches_per_iter = 2 + (info->nbig ? 7 : 0);
+    info->launches_per_iter = 9 + (info->nbig ? 8 : 0);
     return GALP_OK;
 }
 
@@ -663,8 +765,8 @@ int galp_profile_read(galp_ctx *ctx, galp_kernel_times *out)
     std::memset(out, 0, sizeof(*out));
     GALP_CUDA(cudaStreamSynchronize(ctx->stream));
     galp::Profiler &P = ctx->eng.prof;
-    double *ms[3] = {&out->tile_ms, &out->big_pre_ms, &out->big_post_ms};
-    int32_t *cnt[3] = {&out->tile_launches, &out->big_pre_groups, &out->big_post_groups};
+    double *ms[3] = {&out->pipe_ms, &out->big_pre_ms, &out->big_post_ms};
+    int32_t *cnt[3] = {&out->pipe_groups, &out->big_pre_groups, &out->big_post_groups};
     for (int g = 0; g < 3; ++g) {
         for (auto &sp : P.spans[g]) {
             float t = 0.f;

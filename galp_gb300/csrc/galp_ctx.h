@@ -7,7 +7,7 @@
 #include <vector>
 
 #include "../../include/galp.h"
-#include "lp_kernels.cuh"
+#include "lp_pipeline.cuh"
 
 namespace galp {
 
@@ -44,23 +44,23 @@ struct DevBuf {
 // (policies 1/2; batch j = vertices [v0, v1) per OutOfCore::compute_batch_boundaries,
 // label_propagation/src/common/outofcore.cuh:38-60).
 struct Scope {
-    int64_t v0 = 0, v1 = 0;  // vertices
-    int64_t e0 = 0, e1 = 0;  // CSR entries
-    int32_t t0 = 0, nt = 0;  // tiles
-    int32_t b0 = 0, nb = 0;  // big vertices
-    int32_t c0 = 0, nc = 0;  // big insert chunks
-    int32_t s0 = 0, ns = 0;  // big stats chunks
-    int32_t last_v = -1;     // last vertex of the scope that owns runs
-    int64_t table_slots = 0; // global-table slots of the scope's big vertices
-    int64_t occ_slots = 0;   // occupied-list capacity of the scope's big vertices
+    int64_t v0 = 0, v1 = 0;    // vertices
+    int64_t e0 = 0, e1 = 0;    // CSR entries
+    int32_t p0 = 0, np = 0;    // packs of small vertices
+    int32_t m0 = 0, nms = 0, nml = 0, nmx = 0;  // mid (33..256), large (..2048), xl (..12288)
+    int32_t b0 = 0, nb = 0;    // big vertices
+    int32_t c0 = 0, nc = 0;    // big insert chunks
+    int32_t s0 = 0, ns = 0;    // big stats chunks
+    int32_t last_v = -1;       // last vertex of the scope that owns runs
+    int64_t table_slots = 0;   // global-table slots of the scope's big vertices
+    int64_t occ_slots = 0;     // occupied-list capacity of the scope's big vertices
 };
 
-// Static schedule of a graph (host side, built once).
+// Static schedule of a graph (host side, built once): degree buckets per scope.
 struct Schedule {
-    std::vector<uint16_t> vpos;      // slot of each vertex in its tile
-    std::vector<int32_t> tile_v0;    // first vertex of each tile (+ sentinel)
-    std::vector<int32_t> tile_big;   // big-vertex index of single-vertex tiles, else -1
-    std::vector<uint16_t> tile_used; // slots used by each tile
+    std::vector<int32_t> pack_v0;    // first vertex of each pack (<= 32 vertices, <= 32 edges)
+    std::vector<uint8_t> pack_nv;    // vertices in each pack
+    std::vector<int32_t> mid_v;      // per scope: mid vertices, then large vertices
     std::vector<int32_t> big_v;      // vertex of each big entry
     std::vector<int64_t> big_toff;   // table offset, relative to its scope
     std::vector<uint32_t> big_tcap;  // table capacity (power of two >= 2 * degree)
@@ -71,6 +71,7 @@ struct Schedule {
     std::vector<int64_t> schunk_s0, schunk_s1;
     std::vector<Scope> scopes;
     int64_t max_table_slots = 0, max_occ_slots = 0, max_scope_edges = 0, m_big = 0;
+    int64_t max_scope_small = 0, max_scope_mid = 0, max_scope_vertices = 0;
 };
 
 // Build the schedule; scope_starts = first vertex of every scope, then n.
@@ -85,7 +86,7 @@ struct Profiler {
     bool on = false;
     std::vector<cudaEvent_t> pool;
     size_t used = 0;
-    std::vector<std::pair<int, int>> spans[3];  // 0 = tile kernel, 1 = big pre, 2 = big post
+    std::vector<std::pair<int, int>> spans[3];  // 0 = count/scan/resolve, 1 = big pre, 2 = big post
     int mark(cudaStream_t st)
     {
         if (used == pool.size()) {
@@ -109,12 +110,15 @@ struct Engine {
     const int32_t *h_nbr = nullptr;  // caller's host neighbours (streamed for policies 1/2)
     bool registered = false;         // the library pinned h_nbr
     Schedule sched;
-    DevBuf b_nbr[2], b_off, b_vpos, b_tile_v0, b_tile_big, b_tile_used, b_big_v, b_big_toff, b_big_tcap;
+    DevBuf b_nbr[2], b_off, b_pack_v0, b_pack_nv, b_mid_v, b_big_v, b_big_toff, b_big_tcap;
     DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff;
-    DevBuf b_lab0, b_lab1, b_status, b_ctl, b_bstat, b_big_a, b_gkey, b_gcnt, b_occ, b_bad;
-    uint16_t *d_vpos = nullptr;
-    int32_t *d_tile_v0 = nullptr, *d_tile_big = nullptr;
-    uint16_t *d_tile_used = nullptr;
+    DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_gkey, b_gcnt, b_occ, b_bad;
+    DevBuf b_dcnt, b_runbase, b_c0, b_c1, b_kw, b_r, b_run_lab, b_run_cnt, b_tsmall, b_tmid, b_bsum;
+    DevBuf b_dirty, b_changed;  // frontier mode
+    bool frontier = false;
+    int32_t *d_pack_v0 = nullptr;
+    uint8_t *d_pack_nv = nullptr;
+    int32_t *d_mid_v = nullptr;
     int32_t *d_big_v = nullptr;
     int64_t *d_big_toff = nullptr, *d_big_ooff = nullptr;
     uint32_t *d_big_tcap = nullptr;
@@ -122,8 +126,8 @@ struct Engine {
     int64_t *d_chunk_e0 = nullptr, *d_chunk_e1 = nullptr;
     int32_t *d_schunk_big = nullptr;
     int64_t *d_schunk_s0 = nullptr, *d_schunk_s1 = nullptr;
-    unsigned epoch = 0;
-    int tile_grid = 1;
+    int sms = 1;
+    bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
     Profiler prof;
     // out-of-core streaming
     cudaStream_t copy_stream = nullptr;
@@ -133,9 +137,10 @@ struct Engine {
 
     ~Engine();
     int setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_t &h2d);
-    IterArgs args(const Scope &sc) const;
+    IterArgs big_args(const Scope &sc) const;
+    PipeArgs pipe_args(const Scope &sc) const;
     int enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
-                      int32_t *lab_out);
+                      int32_t *lab_out, const uint8_t *dirty = nullptr, int32_t *changed = nullptr);
     int enqueue_run_incore(cudaStream_t st, int niter, long long thr);
     int run_outofcore(cudaStream_t st, int niter, long long thr);
     int enqueue_init(cudaStream_t st, int niter, long long thr);

@@ -55,6 +55,10 @@ struct Ctl {
     int max_iter;               // iterations requested
     int pad1;
     unsigned long long counts[64];  // changes per iteration
+    int tied_small;             // tied vertices listed by the count kernels (per scope)
+    int tied_mid;
+    int changed_n;              // vertices whose label changed (frontier mode)
+    int pad2;
 };
 
 // Per-big-vertex statistics (reset by big_resolve after use).
@@ -108,6 +112,8 @@ struct IterArgs {
     int64_t *big_a;             // run base of each big vertex (written by the scan)
     uint32_t *big_occ;          // occupied-slot list of each big table (capacity = degree)
     const int64_t *big_ooff;    // offset of each big vertex's occupied list
+    const int64_t *runbase;     // run base of every vertex when the scan precedes big_resolve
+    int32_t *changed;           // frontier mode: vertices whose label changes (else null)
 };
 
 __device__ __forceinline__ int pad32(int x) { return (x + 31) & ~31; }
@@ -1093,7 +1099,7 @@ __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
     if (k == 1) {
         label = st.cmin;
     } else {
-        const long long a = p.big_a[bi];
+        const long long a = p.runbase ? p.runbase[v] : p.big_a[bi];
         const long long N = p.ctl->N;
         SummaryQuery sq(k, d, st.rmin, st.rmax);
         int r = resolve_rank(a, d, N, v == p.last_v, sq);
@@ -1113,7 +1119,10 @@ __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
     if (lane == 0) {
         const int32_t old = p.lab_in[v];
         p.lab_out[v] = label;
-        if (label != old) atomicAdd(&p.ctl->changes, 1ull);
+        if (label != old) {
+            atomicAdd(&p.ctl->changes, 1ull);
+            if (p.changed) p.changed[atomicAdd(&p.ctl->changed_n, 1)] = v;
+        }
     }
 }
 

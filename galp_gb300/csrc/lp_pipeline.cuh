@@ -1,0 +1,863 @@
+// lp_pipeline.cuh -- count -> scan -> resolve: the exact label-propagation update
+// without inter-block waiting.
+//
+// One iteration over a scope (whole graph, one out-of-core batch):
+//
+//   count   vertices are degree-bucketed and counted with no dependence between blocks:
+//             small (degree <= 32, and degree 0): one warp per pack of <= 32 label
+//               slots, counting in registers (__match_any_sync on (vertex, label));
+//             mid (33..256): one warp per vertex, shared-memory hash region;
+//             large (257..2048): one CTA per vertex, shared-memory hash region;
+//             big (> 2048): global tables (big_insert/big_stats, lp_kernels.cuh).
+//           Each vertex gets its distinct-label count d; a vertex with a unique
+//           most-frequent label is final and written at once.  A tied vertex leaves a
+//           summary (smallest/largest candidate, their ranks, #candidates, max count)
+//           and its (label, count) runs in a spill area at its own CSR positions,
+//           and joins a list of tied vertices.
+//   scan    exclusive scan of d over the scope's vertices: each vertex's run base,
+//           the position of its first run in the reference's run array
+//           (label_propagation/src/dpp/kernel.cuh:66-82 scatter_indexes).
+//   resolve each tied vertex picks its winner by the reference's positional tie rule
+//           (resolve_rank, lp_resolve.h) from its summary, or from its spilled runs.
+//
+// Spill layout (indexed by CSR position relative to the scope's first entry):
+//   run_lab[e0 + r] label, run_cnt[e0 + r] count of the vertex's r-th run; small
+//   vertices write their runs sorted by label, mid/large vertices their table's
+//   occupied entries unsorted (queried by order statistics).
+#pragma once
+
+#include "lp_kernels.cuh"
+
+namespace galp {
+
+constexpr int kMidSMax = 256;        // mid bucket: 33..256 neighbours, one warp each
+constexpr int kMidSCap = 2 * kMidSMax;
+constexpr int kMidWarps = 8;         // warps (vertices) per mid CTA
+constexpr int kScanBlock = 4096;     // vertices per scan block (256 threads x 16)
+constexpr int kLargeMax = 2048;      // large bucket: 257..2048, one 256-thread CTA each
+constexpr int kXlMax = 12288;        // xl bucket: 2049..12288, one 512-thread CTA each
+constexpr int kXlSlots = 2 * kXlMax; // 192 KB of shared-memory table
+
+struct PipeArgs {
+    const int32_t *nbr;     // neighbour buffer holding CSR entries [nbr_shift, ...)
+    int64_t nbr_shift;
+    const int64_t *off;
+    const int32_t *lab_in;
+    int32_t *lab_out;
+    Ctl *ctl;
+    // static buckets of the scope
+    const int32_t *pack_v0;
+    const uint8_t *pack_nv;
+    int32_t npacks;
+    const int32_t *mid_v;   // mid (33..256), then large (257..2048), then xl (2049..12288) vertices
+    int32_t nmid_s, nmid_l, nmid_x;
+    // per-vertex state (global vertex index)
+    int32_t *dcnt;          // distinct labels
+    int64_t *runbase;       // run base relative to the scope
+    int32_t *sm_c0, *sm_c1; // smallest / largest candidate label
+    int32_t *sm_kw;         // candidates | max count << 16
+    int32_t *sm_r;          // rank of smallest | rank of largest << 16
+    // spill, indexed by CSR position - nbr_shift
+    int32_t *run_lab;
+    uint16_t *run_cnt;
+    // tied lists
+    int32_t *tied_small;
+    int32_t *tied_mid;
+    // scan
+    int64_t v0, v1;         // scope vertices
+    int64_t *bsum;          // per scan block
+    int32_t last_v;
+    // frontier mode (null = every vertex is recounted and no changes are recorded)
+    const uint8_t *dirty;   // 1 = a neighbour's label changed in the previous iteration
+    int32_t *changed;       // vertices whose label changes in this iteration
+};
+
+__device__ __forceinline__ void count_change(unsigned long long &changes, int32_t nl, int32_t old)
+{
+    changes += (nl != old);
+}
+
+// Record a changed vertex for the next iteration's frontier (single thread).
+__device__ __forceinline__ void note_change(const PipeArgs &p, int32_t v, int32_t nl, int32_t old)
+{
+    if (p.changed && nl != old) p.changed[atomicAdd(&p.ctl->changed_n, 1)] = v;
+}
+
+__device__ __forceinline__ void flush_changes(unsigned long long changes, Ctl *ctl)
+{
+    unsigned long long c = changes;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) c += __shfl_xor_sync(kFull, c, off);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&ctl->changes, c);
+}
+
+// warp-aggregated append of the lanes with `pred` to list[ctr++]
+__device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t *list, int *ctr)
+{
+    const unsigned m = __ballot_sync(kFull, pred);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == __ffs(m) - 1) base = atomicAdd(ctr, __popc(m));
+    base = __shfl_sync(kFull, base, __ffs(m) - 1);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1))] = value;
+}
+
+// warp-level version of note_change (all lanes call it)
+__device__ __forceinline__ void warp_note_changes(const PipeArgs &p, bool changed, int32_t v)
+{
+    if (p.changed) warp_append(changed, v, p.changed, &p.ctl->changed_n);
+}
+
+// ---------------------------------------------------------------------------
+// small vertices: one warp per pack
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
+{
+    if (!ctl_active(p.ctl)) return;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long changes = 0;
+    for (int pk = gw; pk < p.npacks; pk += nw) {
+        const int v0 = p.pack_v0[pk], nv = p.pack_nv[pk];
+        // vertex lanes: offsets, degrees, slot positions
+        const bool vl = lane < nv;
+        const int v = v0 + lane;
+        if (p.dirty && !__any_sync(kFull, vl && p.dirty[v])) {
+            // no label around this pack changed: counts and summaries carry over; labels
+            // of untied vertices stay, tied vertices are resolved again (run bases move)
+            bool tied = false;
+            if (vl && (__ldg(&p.off[v + 1]) > __ldg(&p.off[v]))) tied = (p.sm_kw[v] & 0xFFFF) > 1;
+            if (vl && !tied) p.lab_out[v] = __ldg(&p.lab_in[v]);
+            warp_append(tied, v, p.tied_small, &p.ctl->tied_small);
+            continue;
+        }
+        const int64_t o0 = vl ? __ldg(&p.off[v]) : 0;
+        const int deg = vl ? (int)(__ldg(&p.off[v + 1]) - o0) : 0;
+        int pos = deg;
+#pragma unroll
+        for (int s = 1; s < 32; s <<= 1) {
+            const int o = __shfl_up_sync(kFull, pos, s);
+            if (lane >= s) pos += o;
+        }
+        const int total = __shfl_sync(kFull, pos, 31);
+        pos -= deg;  // exclusive
+        // slot lanes: owner vertex lane j, CSR entry, label
+        const bool valid = lane < total;
+        // owner of slot `lane`: the last vertex lane whose first slot is <= lane
+        // (positions are non-decreasing over the vertex lanes; binary lifting)
+        int j = 0;
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+            const int t = j + step;
+            const int pt = __shfl_sync(kFull, pos, t < 32 ? t : 31);
+            if (t < nv && pt <= lane) j = t;
+        }
+        if (!valid) j = 0;
+        const int64_t oj = __shfl_sync(kFull, o0, j);
+        const int pj = __shfl_sync(kFull, pos, j);
+        int lab = 0;
+        if (valid) lab = __ldg(&p.lab_in[__ldg(&p.nbr[oj + (lane - pj) - p.nbr_shift])]);
+        // count in registers: segments of lanes per vertex
+        const unsigned long long key =
+            valid ? (((unsigned long long)(unsigned)j << 32) | (unsigned)lab) : (0xFFFFFFFF00000000ull | (unsigned)lane);
+        const unsigned eq = __match_any_sync(kFull, key);
+        const unsigned vm = __match_any_sync(kFull, valid ? j : (-1 - lane));
+        const int cnt = __popc(eq);
+        const bool leader = valid && ((__ffs(eq) - 1) == lane);
+        const unsigned lm = __ballot_sync(kFull, leader);
+        const int first = __ffs(vm) - 1, last = 31 - __clz(vm);
+        const int W = seg_max(valid ? cnt : 0, lane, first, last);
+        const bool cand = leader && cnt == W;
+        const unsigned cm = __ballot_sync(kFull, cand);
+        const int k = __popc(cm & vm);
+        const int d = __popc(lm & vm);
+        int cmin, cmax, rmin = 0, rmax = 0;
+        if (__all_sync(kFull, !valid || k == 1)) {
+            const unsigned m = cm & vm;
+            cmin = cmax = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : lane);
+        } else {
+            // sort the pack by (vertex, label): runs become adjacent and ascending
+            unsigned long long sk = key;
+            int sc = valid ? cnt : 0;
+#pragma unroll
+            for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                    const unsigned long long ok = __shfl_xor_sync(kFull, sk, jj);
+                    const int oc = __shfl_xor_sync(kFull, sc, jj);
+                    const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
+                    if ((lower == up) ? (ok < sk) : (ok > sk)) {
+                        sk = ok;
+                        sc = oc;
+                    }
+                }
+            }
+            const int slab = (int)(unsigned)sk;
+            const int prev = __shfl_up_sync(kFull, slab, 1);
+            const bool head = valid && (lane == first || prev != slab);
+            const unsigned hm = __ballot_sync(kFull, head) & vm;
+            const int rank = __popc(hm & ((1u << lane) - 1));
+            const unsigned cr = __ballot_sync(kFull, head && sc == W) & vm;
+            const bool tied_v = __popc(cr) > 1;
+            if (head && tied_v) {  // spill the sorted runs of tied vertices
+                const int64_t e = oj - p.nbr_shift + rank;
+                p.run_lab[e] = slab;
+                p.run_cnt[e] = (uint16_t)sc;
+            }
+            const int lo = cr ? (__ffs(cr) - 1) : lane, hi = cr ? (31 - __clz(cr)) : lane;
+            cmin = __shfl_sync(kFull, slab, lo);
+            cmax = __shfl_sync(kFull, slab, hi);
+            rmin = __popc(hm & ((1u << lo) - 1));
+            rmax = __popc(hm & ((1u << hi) - 1));
+        }
+        // results live at each vertex's first slot lane; bring them to the vertex lanes
+        const int src = (vl && deg > 0) ? pos : lane;
+        const int d_v = __shfl_sync(kFull, d, src);
+        const int k_v = __shfl_sync(kFull, k, src);
+        const int W_v = __shfl_sync(kFull, W, src);
+        const int c0_v = __shfl_sync(kFull, cmin, src);
+        const int c1_v = __shfl_sync(kFull, cmax, src);
+        const int r0_v = __shfl_sync(kFull, rmin, src);
+        const int r1_v = __shfl_sync(kFull, rmax, src);
+        const bool tied = vl && deg > 0 && k_v > 1;
+        bool chg = false;
+        if (vl) {
+            p.dcnt[v] = deg > 0 ? d_v : 0;
+            const int32_t old = __ldg(&p.lab_in[v]);
+            if (deg > 0) p.sm_kw[v] = k_v | (W_v << 16);
+            if (!tied) {
+                const int32_t nl = deg > 0 ? c0_v : old;
+                p.lab_out[v] = nl;
+                count_change(changes, nl, old);
+                chg = nl != old;
+            } else {
+                p.sm_c0[v] = c0_v;
+                p.sm_c1[v] = c1_v;
+                p.sm_r[v] = r0_v | (r1_v << 16);
+            }
+        }
+        warp_append(tied, v, p.tied_small, &p.ctl->tied_small);
+        warp_note_changes(p, chg, v);
+    }
+    flush_changes(changes, p.ctl);
+}
+
+// ---------------------------------------------------------------------------
+// mid and large vertices: hash region in shared memory
+// ---------------------------------------------------------------------------
+
+// Summary of one vertex's table region, computed by a group of threads.  `red` is a
+// reduction helper over the group.
+template <class Red>
+__device__ void table_summary(const uint32_t *key, const uint32_t *cnt, int cap, int gtid, int gsize, Red red,
+                              int &d, int &W, int &k, int &cmin, int &cmax, int &rmin, int &rmax)
+{
+    int dp = 0, wp = 0;
+    for (int s = gtid; s < cap; s += gsize)
+        if (key[s] != kEmpty) {
+            dp++;
+            wp = max(wp, (int)cnt[s]);
+        }
+    d = red.sum(dp);
+    W = red.max(wp);
+    int kp = 0, mn = INT_MAX, mx = -1;
+    for (int s = gtid; s < cap; s += gsize)
+        if (key[s] != kEmpty && (int)cnt[s] == W) {
+            kp++;
+            mn = min(mn, (int)key[s]);
+            mx = max(mx, (int)key[s]);
+        }
+    k = red.sum(kp);
+    cmin = red.min(mn);
+    cmax = red.max(mx);
+    rmin = rmax = 0;
+    if (k > 1) {
+        int a0 = 0, a1 = 0;
+        for (int s = gtid; s < cap; s += gsize)
+            if (key[s] != kEmpty) {
+                a0 += (int)key[s] < cmin;
+                a1 += (int)key[s] < cmax;
+            }
+        rmin = red.sum(a0);
+        rmax = red.sum(a1);
+    }
+}
+
+struct WarpRed {
+    __device__ int sum(int x) const { return __reduce_add_sync(kFull, x); }
+    __device__ int max(int x) const { return __reduce_max_sync(kFull, x); }
+    __device__ int min(int x) const { return __reduce_min_sync(kFull, x); }
+};
+
+template <int THREADS>
+struct BlockRedT {
+    int *buf;  // THREADS / 32 ints
+    __device__ int combine(int x, int op) const
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        int w = op == 0 ? __reduce_add_sync(kFull, x) : op == 1 ? __reduce_max_sync(kFull, x) : __reduce_min_sync(kFull, x);
+        __syncthreads();
+        if (lane == 0) buf[warp] = w;
+        __syncthreads();
+        int r = buf[0];
+        for (int i = 1; i < THREADS / 32; ++i) r = op == 0 ? r + buf[i] : op == 1 ? ::max(r, buf[i]) : ::min(r, buf[i]);
+        return r;
+    }
+    __device__ int sum(int x) const { return combine(x, 0); }
+    __device__ int max(int x) const { return combine(x, 1); }
+    __device__ int min(int x) const { return combine(x, 2); }
+};
+
+// Write the occupied (label, count) entries of a tied vertex's region to its spill
+// positions (unsorted), by one warp.
+__device__ void spill_region_warp(const uint32_t *key, const uint32_t *cnt, int cap, int32_t *rl, uint16_t *rc,
+                                  int lane)
+{
+    int base = 0;
+    for (int s0 = 0; s0 < cap; s0 += 32) {
+        const int s = s0 + lane;
+        const bool occ = s < cap && key[s] != kEmpty;
+        const unsigned m = __ballot_sync(kFull, occ);
+        if (occ) {
+            const int at = base + __popc(m & ((1u << lane) - 1));
+            rl[at] = (int32_t)key[s];
+            rc[at] = (uint16_t)cnt[s];
+        }
+        base += __popc(m);
+    }
+}
+
+__global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
+{
+    __shared__ uint32_t skey[kMidWarps][kMidSCap];
+    __shared__ uint32_t scnt[kMidWarps][kMidSCap];
+    if (!ctl_active(p.ctl)) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kMidWarps + w;
+    const int nw = gridDim.x * kMidWarps;
+    unsigned long long changes = 0;
+    uint32_t *key = skey[w], *cnt = scnt[w];
+    for (int i = gw; i < p.nmid_s; i += nw) {
+        const int v = p.mid_v[i];
+        if (p.dirty && !p.dirty[v]) {
+            if (lane == 0) {
+                if ((p.sm_kw[v] & 0xFFFF) > 1) p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+                else p.lab_out[v] = __ldg(&p.lab_in[v]);
+            }
+            continue;
+        }
+        const int64_t o0 = __ldg(&p.off[v]);
+        const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
+        const int cap = 2 * pad32(deg);
+        for (int s = lane; s < cap; s += 32) {
+            key[s] = kEmpty;
+            cnt[s] = 0;
+        }
+        __syncwarp();
+        constexpr int PER = kMidSMax / 32;
+        int nb[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int e = lane + u * 32;
+            nb[u] = (e < deg) ? __ldg(&p.nbr[o0 + e - p.nbr_shift]) : -1;
+        }
+        uint32_t lb[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[u]]) : kEmpty;
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            // lanes holding the same label add once (heavy labels would serialise)
+            const unsigned same = __match_any_sync(kFull, lb[u]);
+            if (lb[u] == kEmpty || lane != __ffs(same) - 1) continue;
+            uint32_t h = hslot(lb[u], (uint32_t)cap);
+            for (;;) {
+                const uint32_t prev = atomicCAS(&key[h], kEmpty, lb[u]);
+                if (prev == kEmpty || prev == lb[u]) {
+                    atomicAdd(&cnt[h], (uint32_t)__popc(same));
+                    break;
+                }
+                h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
+            }
+        }
+        __syncwarp();
+        int d, W, k, cmin, cmax, rmin, rmax;
+        table_summary(key, cnt, cap, lane, 32, WarpRed{}, d, W, k, cmin, cmax, rmin, rmax);
+        const bool tied = k > 1;
+        if (tied) spill_region_warp(key, cnt, cap, p.run_lab + (o0 - p.nbr_shift), p.run_cnt + (o0 - p.nbr_shift), lane);
+        if (lane == 0) {
+            p.dcnt[v] = d;
+            p.sm_kw[v] = k | (W << 16);
+            const int32_t old = __ldg(&p.lab_in[v]);
+            if (!tied) {
+                p.lab_out[v] = cmin;
+                count_change(changes, cmin, old);
+                note_change(p, v, cmin, old);
+            } else {
+                p.sm_c0[v] = cmin;
+                p.sm_c1[v] = cmax;
+                p.sm_r[v] = rmin | (rmax << 16);
+                p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+            }
+        }
+        __syncwarp();
+    }
+    flush_changes(changes, p.ctl);
+}
+
+// One CTA of THREADS threads per vertex of degree <= SLOTS/2 (label slots in dynamic
+// shared memory: keys then counts), for the vertices mid_v[first .. first + count).
+template <int THREADS, int SLOTS>
+__global__ void __launch_bounds__(THREADS) count_cta_kernel(PipeArgs p, int first, int count)
+{
+    extern __shared__ __align__(16) uint32_t cta_smem[];
+    uint32_t *key = cta_smem, *cnt = cta_smem + SLOTS;
+    __shared__ int red[THREADS / 32];
+    if (!ctl_active(p.ctl)) return;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned long long changes = 0;
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        const int v = p.mid_v[first + i];
+        if (p.dirty && !p.dirty[v]) {
+            if (tid == 0) {
+                if ((p.sm_kw[v] & 0xFFFF) > 1) p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+                else p.lab_out[v] = __ldg(&p.lab_in[v]);
+            }
+            continue;
+        }
+        const int64_t o0 = __ldg(&p.off[v]);
+        const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
+        const int cap = 2 * pad32(deg);
+        for (int s = tid; s < cap; s += THREADS) {
+            key[s] = kEmpty;
+            cnt[s] = 0;
+        }
+        __syncthreads();
+        // gather in rounds of PER loads per thread in flight together
+        constexpr int PER = 8;
+        for (int base = 0; base < deg; base += THREADS * PER) {
+            int nb[PER];
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int e = base + tid + u * THREADS;
+                nb[u] = (e < deg) ? __ldg(&p.nbr[o0 + e - p.nbr_shift]) : -1;
+            }
+            uint32_t lb[PER];
+#pragma unroll
+            for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[u]]) : kEmpty;
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                // lanes holding the same label add once (heavy labels would serialise)
+                const unsigned same = __match_any_sync(kFull, lb[u]);
+                if (lb[u] == kEmpty || lane != __ffs(same) - 1) continue;
+                uint32_t h = hslot(lb[u], (uint32_t)cap);
+                for (;;) {
+                    const uint32_t prev = atomicCAS(&key[h], kEmpty, lb[u]);
+                    if (prev == kEmpty || prev == lb[u]) {
+                        atomicAdd(&cnt[h], (uint32_t)__popc(same));
+                        break;
+                    }
+                    h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
+                }
+            }
+        }
+        __syncthreads();
+        int d, W, k, cmin, cmax, rmin, rmax;
+        table_summary(key, cnt, cap, tid, THREADS, BlockRedT<THREADS>{red}, d, W, k, cmin, cmax, rmin, rmax);
+        const bool tied = k > 1;
+        if (tied && warp == 0)
+            spill_region_warp(key, cnt, cap, p.run_lab + (o0 - p.nbr_shift), p.run_cnt + (o0 - p.nbr_shift), lane);
+        if (tid == 0) {
+            p.dcnt[v] = d;
+            p.sm_kw[v] = k | (W << 16);
+            const int32_t old = __ldg(&p.lab_in[v]);
+            if (!tied) {
+                p.lab_out[v] = cmin;
+                count_change(changes, cmin, old);
+                note_change(p, v, cmin, old);
+            } else {
+                p.sm_c0[v] = cmin;
+                p.sm_c1[v] = cmax;
+                p.sm_r[v] = rmin | (rmax << 16);
+                p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+            }
+        }
+        __syncthreads();
+    }
+    flush_changes(changes, p.ctl);
+}
+
+// big vertices: distinct counts into dcnt before the scan
+__global__ void big_dcnt_kernel(IterArgs a, int32_t *dcnt)
+{
+    if (!ctl_active(a.ctl)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nbig; i += gridDim.x * blockDim.x)
+        dcnt[a.big_v[a.b0 + i]] = a.bstat[a.b0 + i].d;
+}
+
+// ---------------------------------------------------------------------------
+// scan of distinct counts -> run bases (reduce, spine, apply)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTB) scan_reduce_kernel(PipeArgs p)
+{
+    __shared__ long long ws[kNW];
+    if (!ctl_active(p.ctl)) return;
+    const int64_t b0 = p.v0 + (int64_t)blockIdx.x * kScanBlock;
+    long long s = 0;
+    for (int i = threadIdx.x; i < kScanBlock; i += kTB) {
+        const int64_t v = b0 + i;
+        if (v < p.v1) s += p.dcnt[v];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(kFull, s, off);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long t = 0;
+        for (int w = 0; w < kNW; ++w) t += ws[w];
+        p.bsum[blockIdx.x] = t;
+    }
+}
+
+// one CTA: exclusive scan of the block sums in place; total -> ctl->N
+__global__ void __launch_bounds__(kTB) scan_spine_kernel(PipeArgs p, int nblocks)
+{
+    __shared__ long long ws[kNW];
+    __shared__ long long carry;
+    if (!ctl_active(p.ctl)) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nblocks; base += kTB) {
+        const int i = base + threadIdx.x;
+        const long long x = i < nblocks ? p.bsum[i] : 0;
+        long long incl = x;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const long long o = __shfl_up_sync(kFull, incl, off);
+            if (lane >= off) incl += o;
+        }
+        if (lane == 31) ws[warp] = incl;
+        __syncthreads();
+        long long wb = 0, tot = 0;
+        for (int w = 0; w < kNW; ++w) {
+            if (w < warp) wb += ws[w];
+            tot += ws[w];
+        }
+        const long long c = carry;
+        if (i < nblocks) p.bsum[i] = c + wb + incl - x;
+        __syncthreads();
+        if (threadIdx.x == 0) carry = c + tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) p.ctl->N = carry;
+}
+
+__global__ void __launch_bounds__(kTB) scan_apply_kernel(PipeArgs p)
+{
+    __shared__ long long ws[kNW];
+    if (!ctl_active(p.ctl)) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int PER = kScanBlock / kTB;
+    const int64_t b0 = p.v0 + (int64_t)blockIdx.x * kScanBlock + (int64_t)threadIdx.x * PER;
+    int x[PER];
+    long long s = 0;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        x[u] = (b0 + u < p.v1) ? p.dcnt[b0 + u] : 0;
+        s += x[u];
+    }
+    long long incl = s;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const long long o = __shfl_up_sync(kFull, incl, off);
+        if (lane >= off) incl += o;
+    }
+    if (lane == 31) ws[warp] = incl;
+    __syncthreads();
+    long long wb = 0;
+    for (int w = 0; w < warp; ++w) wb += ws[w];
+    long long run = p.bsum[blockIdx.x] + wb + incl - s;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        if (b0 + u < p.v1) p.runbase[b0 + u] = run;
+        run += x[u];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// resolution of tied vertices
+// ---------------------------------------------------------------------------
+
+// Sorted spilled runs of a small vertex, scanned by one thread.
+struct SpillRunQuery {
+    const int32_t *lab;
+    const uint16_t *cnt;
+    int d, W;
+    __device__ int first_ge(int64_t x) const
+    {
+        for (int r = (int)(x < 0 ? 0 : x); r < d; ++r)
+            if ((int)cnt[r] == W) return r;
+        return -1;
+    }
+    __device__ int last_lt(int64_t y) const
+    {
+        for (int r = (int)(y < d ? y : d) - 1; r >= 0; --r)
+            if ((int)cnt[r] == W) return r;
+        return -1;
+    }
+    __device__ int tile_pick(int64_t) const { return -1; }  // d <= 32 never spans a tile
+};
+
+__global__ void __launch_bounds__(kTB) resolve_small_kernel(PipeArgs p)
+{
+    if (!ctl_active(p.ctl)) return;
+    const int nt = *((volatile int *)&p.ctl->tied_small);
+    unsigned long long changes = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+        const int v = p.tied_small[i];
+        const int kw = p.sm_kw[v], rr = p.sm_r[v];
+        const int k = kw & 0xFFFF, W = kw >> 16, rmin = rr & 0xFFFF, rmax = rr >> 16;
+        const int d = p.dcnt[v];
+        const long long a = p.runbase[v];
+        const long long N = p.ctl->N;
+        const bool is_last = v == p.last_v;
+        SummaryQuery q(k, d, rmin, rmax);
+        int r = resolve_rank(a, d, N, is_last, q);
+        int32_t nl;
+        if (!q.fail && r == rmin) {
+            nl = p.sm_c0[v];
+        } else if (!q.fail && r == rmax) {
+            nl = p.sm_c1[v];
+        } else {
+            const int64_t e = __ldg(&p.off[v]) - p.nbr_shift;
+            SpillRunQuery sq{p.run_lab + e, p.run_cnt + e, d, W};
+            if (q.fail) r = resolve_rank(a, d, N, is_last, sq);
+            nl = p.run_lab[e + r];
+        }
+        const int32_t old = __ldg(&p.lab_in[v]);
+        p.lab_out[v] = nl;
+        count_change(changes, nl, old);
+        note_change(p, v, nl, old);
+    }
+    flush_changes(changes, p.ctl);
+}
+
+// Unsorted spilled (label, count) entries of a mid/large vertex, one warp.
+struct SpillTableQuery {
+    const int32_t *lab;
+    const uint16_t *cnt;
+    int d, W, rmin, rmax;
+    int *hist;
+    int lane;
+    __device__ uint32_t select(int x)
+    {
+        uint32_t prefix = 0;
+        int remaining = x;
+        for (int shift = 24; shift >= 0; shift -= 8) {
+            for (int b = lane; b < 256; b += 32) hist[b] = 0;
+            __syncwarp();
+            const uint32_t hi_mask = (shift == 24) ? 0u : (0xFFFFFFFFu << (shift + 8));
+            for (int i = lane; i < d; i += 32) {
+                const uint32_t k = (uint32_t)lab[i];
+                if ((k & hi_mask) == (prefix & hi_mask)) atomicAdd(&hist[(k >> shift) & 255], 1);
+            }
+            __syncwarp();
+            int c[8];
+            int local = 0;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                c[i] = hist[lane * 8 + i];
+                local += c[i];
+            }
+            int incl = local;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const int o = __shfl_up_sync(kFull, incl, off);
+                if (lane >= off) incl += o;
+            }
+            const int excl = incl - local;
+            const unsigned who = __ballot_sync(kFull, remaining >= excl && remaining < incl);
+            const int src = who ? (__ffs(who) - 1) : 31;
+            int digit = 0, before = 0;
+            if (lane == src) {
+                int acc = excl, i = 0;
+                for (; i < 7; ++i) {
+                    if (remaining < acc + c[i]) break;
+                    acc += c[i];
+                }
+                digit = lane * 8 + i;
+                before = acc;
+            }
+            digit = __shfl_sync(kFull, digit, src);
+            before = __shfl_sync(kFull, before, src);
+            prefix |= (uint32_t)digit << shift;
+            remaining -= before;
+            __syncwarp();
+        }
+        return prefix;
+    }
+    __device__ int rank_of(uint32_t c) const
+    {
+        int n = 0;
+        for (int i = lane; i < d; i += 32) n += (uint32_t)lab[i] < c;
+        return __reduce_add_sync(kFull, n);
+    }
+    __device__ int first_ge(int64_t x)
+    {
+        if (x >= d) return -1;
+        if (x <= rmin) return rmin;
+        const uint32_t L = select((int)x);
+        uint32_t best = kEmpty;
+        for (int i = lane; i < d; i += 32) {
+            const uint32_t k = (uint32_t)lab[i];
+            if ((int)cnt[i] == W && k >= L && k < best) best = k;
+        }
+        best = __reduce_min_sync(kFull, best);
+        return best == kEmpty ? -1 : rank_of(best);
+    }
+    __device__ int last_lt(int64_t y)
+    {
+        if (y > rmax) return rmax;
+        if (y <= rmin) return -1;
+        const uint32_t L = select((int)y);
+        int best = -1;
+        for (int i = lane; i < d; i += 32) {
+            const uint32_t k = (uint32_t)lab[i];
+            if ((int)cnt[i] == W && k < L && (int)k > best) best = (int)k;
+        }
+        best = __reduce_max_sync(kFull, best);
+        return best < 0 ? -1 : rank_of((uint32_t)best);
+    }
+    // Among candidates of rank in [lo, lo + kTile) (a whole tile), the one of highest
+    // tile_priority; ranks by full passes (only vertices of > 4352 distinct labels
+    // whose last tile holds no candidate get here).
+    __device__ int tile_pick(int64_t lo)
+    {
+        int best = -1, bestr = -1;
+        for (int i0 = 0; i0 < d; i0 += 32) {
+            const int i = i0 + lane;
+            const bool c = i < d && (int)cnt[i] == W;
+            unsigned m = __ballot_sync(kFull, c);
+            while (m) {
+                const int src = __ffs(m) - 1;
+                m &= m - 1;
+                const uint32_t lab_c = (uint32_t)__shfl_sync(kFull, i < d ? lab[i] : 0, src);
+                const int r = rank_of(lab_c);
+                if (r >= lo && r < lo + kTile && tile_priority(r - lo) > best) {
+                    best = tile_priority(r - lo);
+                    bestr = r;
+                }
+            }
+        }
+        return bestr;
+    }
+};
+
+__global__ void __launch_bounds__(kTB) resolve_mid_kernel(PipeArgs p)
+{
+    __shared__ int hist[kNW][256];
+    if (!ctl_active(p.ctl)) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int nt = *((volatile int *)&p.ctl->tied_mid);
+    unsigned long long changes = 0;
+    for (int i = blockIdx.x * kNW + w; i < nt; i += gridDim.x * kNW) {
+        const int v = p.tied_mid[i];
+        const int kw = p.sm_kw[v], rr = p.sm_r[v];
+        const int k = kw & 0xFFFF, W = kw >> 16, rmin = rr & 0xFFFF, rmax = rr >> 16;
+        const int d = p.dcnt[v];
+        const long long a = p.runbase[v];
+        const long long N = p.ctl->N;
+        const bool is_last = v == p.last_v;
+        SummaryQuery q(k, d, rmin, rmax);
+        int r = resolve_rank(a, d, N, is_last, q);
+        int32_t nl;
+        if (!q.fail && r == rmin) {
+            nl = p.sm_c0[v];
+        } else if (!q.fail && r == rmax) {
+            nl = p.sm_c1[v];
+        } else {
+            const int64_t e = __ldg(&p.off[v]) - p.nbr_shift;
+            SpillTableQuery tq{p.run_lab + e, p.run_cnt + e, d, W, rmin, rmax, hist[w], lane};
+            if (q.fail) r = resolve_rank(a, d, N, is_last, tq);
+            nl = (r == rmin) ? p.sm_c0[v] : (r == rmax) ? p.sm_c1[v] : (int32_t)tq.select(r);
+        }
+        if (lane == 0) {
+            const int32_t old = __ldg(&p.lab_in[v]);
+            p.lab_out[v] = nl;
+            count_change(changes, nl, old);
+            note_change(p, v, nl, old);
+        }
+    }
+    flush_changes(changes, p.ctl);
+}
+
+// Frontier: mark the neighbours of every vertex that changed in the previous iteration
+// (the graph is symmetric, so they are exactly the vertices whose neighbour labels
+// changed).  One warp per changed vertex.
+__global__ void __launch_bounds__(kTB) mark_dirty_kernel(const int64_t *off, const int32_t *nbr,
+                                                         const int32_t *changed, int nchanged_cap, Ctl *ctl,
+                                                         uint8_t *dirty)
+{
+    const int lane = threadIdx.x & 31;
+    const int nc = min(*((volatile int *)&ctl->changed_n), nchanged_cap);
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nc; i += (gridDim.x * blockDim.x) >> 5) {
+        const int u = changed[i];
+        const int64_t e0 = off[u], e1 = off[u + 1];
+        for (int64_t e = e0 + lane; e < e1; e += 32) dirty[nbr[e]] = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// first iteration on strictly increasing adjacency lists
+// ---------------------------------------------------------------------------
+//
+// With labels = vertex IDs (the reference's initialize_labels, dpp/kernel.cuh:15-22) and
+// every adjacency list strictly increasing, each vertex's neighbour labels are distinct
+// and already sorted: d = degree, every run has count 1 (all are candidates), the run
+// base of v is offsets[v] and the scope holds N = m runs.  The winning run r follows
+// from the closed form alone and its label is the neighbour ID at offsets[v] + r.
+
+// Every distinct label is a candidate (k == d).
+struct AllCandidates {
+    int64_t d;
+    __device__ int first_ge(int64_t x) const { return x < d ? (int)(x < 0 ? 0 : x) : -1; }
+    __device__ int last_lt(int64_t y) const { return y > 0 ? (int)((y < d ? y : d) - 1) : -1; }
+    __device__ int tile_pick(int64_t lo) const { return (int)(lo + kTile - 1); }
+};
+
+__global__ void __launch_bounds__(kTB) first_iteration_kernel(PipeArgs p, int64_t n, int64_t m)
+{
+    if (!ctl_active(p.ctl)) return;
+    unsigned long long changes = 0;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o0 = __ldg(&p.off[v]);
+        const int64_t deg = __ldg(&p.off[v + 1]) - o0;
+        const int32_t old = __ldg(&p.lab_in[v]);
+        int32_t nl = old;
+        if (deg > 0) {
+            AllCandidates q{deg};
+            const int r = resolve_rank(o0, deg, m, v == p.last_v, q);
+            nl = __ldg(&p.nbr[o0 + r]);
+        }
+        p.lab_out[v] = nl;
+        count_change(changes, nl, old);
+        note_change(p, (int32_t)v, nl, old);
+    }
+    flush_changes(changes, p.ctl);
+}
+
+// Sets *bad when some adjacency list is not strictly increasing.
+__global__ void adjacency_order_kernel(const int64_t *off, const int32_t *nbr, int64_t n, int *bad)
+{
+    int b = 0;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e1 = off[v + 1];
+        for (int64_t e = off[v] + 1; e < e1 && !b; ++e)
+            if (nbr[e] <= nbr[e - 1]) b = 1;
+    }
+    if (__any_sync(kFull, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+}  // namespace galp

@@ -7,13 +7,13 @@ from . import load_library
 
 
 class SchedInfo(ctypes.Structure):
-    _fields_ = [("n", ctypes.c_int64), ("m", ctypes.c_int64), ("m_big", ctypes.c_int64), ("ntiles", ctypes.c_int64),
-                ("nbig", ctypes.c_int64), ("table_slots", ctypes.c_int64), ("launches_per_iter", ctypes.c_int32),
-                ("pad", ctypes.c_int32)]
+    _fields_ = [("n", ctypes.c_int64), ("m", ctypes.c_int64), ("m_big", ctypes.c_int64), ("npacks", ctypes.c_int64),
+                ("nmid", ctypes.c_int64), ("nlarge", ctypes.c_int64), ("nbig", ctypes.c_int64),
+                ("table_slots", ctypes.c_int64), ("launches_per_iter", ctypes.c_int32), ("pad", ctypes.c_int32)]
 
 
 class KernelTimes(ctypes.Structure):
-    _fields_ = [("tile_ms", ctypes.c_double), ("tile_launches", ctypes.c_int32), ("big_pre_groups", ctypes.c_int32),
+    _fields_ = [("pipe_ms", ctypes.c_double), ("pipe_groups", ctypes.c_int32), ("big_pre_groups", ctypes.c_int32),
                 ("big_pre_ms", ctypes.c_double), ("big_post_ms", ctypes.c_double),
                 ("big_post_groups", ctypes.c_int32), ("pad", ctypes.c_int32)]
 

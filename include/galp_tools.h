@@ -17,20 +17,22 @@ extern "C" {
 
 typedef struct {
     int64_t n, m;          /* vertices, CSR entries */
-    int64_t m_big;         /* CSR entries of vertices above the tile capacity (global-table path) */
-    int64_t ntiles;        /* vertex tiles of the single-pass kernel */
+    int64_t m_big;         /* CSR entries of vertices above 2048 neighbours (global-table path) */
+    int64_t npacks;        /* packs of vertices with <= 32 neighbours (one warp each) */
+    int64_t nmid;          /* vertices with 33..256 neighbours (one warp each) */
+    int64_t nlarge;        /* vertices with 257..2048 neighbours (one CTA each) */
     int64_t nbig;          /* vertices on the global-table path */
-    int64_t table_slots;   /* global hash-table slots of those vertices */
-    int32_t launches_per_iter; /* kernels launched per iteration */
+    int64_t table_slots;   /* global hash-table slots of those vertices (largest scope) */
+    int32_t launches_per_iter; /* kernels launched per iteration (upper bound) */
     int32_t pad;
 } galp_sched_info;
 
 typedef struct {
-    double tile_ms;        /* lp_tile_kernel: summed device time */
-    int32_t tile_launches;
+    double pipe_ms;        /* count + scan + resolve kernels: summed device time */
+    int32_t pipe_groups;   /* scopes timed */
     int32_t big_pre_groups;
-    double big_pre_ms;     /* big_insert + big_stats: summed device time */
-    double big_post_ms;    /* big_resolve + big_clear */
+    double big_pre_ms;     /* big_insert + big_stats + big_dcnt: summed device time */
+    double big_post_ms;    /* big_resolve + big_clear + big_reset */
     int32_t big_post_groups;
     int32_t pad;
 } galp_kernel_times;

@@ -67,11 +67,51 @@ def test_lfr_small(method):
     assert np.array_equal(got, want)
 
 
-def test_rmat_with_big_vertices():
-    # scale 15: many degree-1 vertices and hubs above the 2048-slot tile
+def test_rmat_with_hubs():
+    # scale 15: degree-1 vertices up to hubs of a few thousand (every counting bucket
+    # below the global tables); scale 17: one hub above 12288 (global-table path)
     g = galp_gb300.generate_rmat(15, 16, seed=11)
     assert g.degrees().max() > 2048
     _check_every_iteration(g, 4)
+    g = galp_gb300.generate_rmat(17, 16, seed=11)
+    assert g.degrees().max() > 12288
+    _check_every_iteration(g, 3)
+
+
+def _bipartite(sizes):
+    """Disjoint complete bipartite blocks K(a, b): many exact ties at every degree."""
+    src, dst, base = [], [], 0
+    for a, b in sizes:
+        left = np.arange(base, base + a)
+        right = np.arange(base + a, base + a + b)
+        s = np.repeat(left, b)
+        d = np.tile(right, a)
+        src += [s, d]
+        dst += [d, s]
+        base += a + b
+    src, dst = np.concatenate(src), np.concatenate(dst)
+    order = np.lexsort((dst, src))
+    src, dst = src[order], dst[order]
+    off = np.zeros(base + 1, np.int64)
+    np.add.at(off, src + 1, 1)
+    return galp_gb300.Graph(np.cumsum(off), dst.astype(np.int32))
+
+
+def test_xl_and_global_table_ties():
+    # right sides of degree 2500 (one CTA, 192 KB table) and 13000 (global table)
+    g = _bipartite([(2500, 40), (13000, 3), (5000, 5)])
+    _check_every_iteration(g, 3)
+
+
+def test_unsorted_adjacency():
+    # adjacency lists in arbitrary order: the first iteration takes the general path
+    g = galp_gb300.generate_lfr(20000, seed=12)
+    rng = np.random.default_rng(3)
+    nbr = g.neighbors.copy()
+    for v in range(g.n):
+        lo, hi = g.offsets[v], g.offsets[v + 1]
+        nbr[lo:hi] = rng.permutation(nbr[lo:hi])
+    _check_every_iteration(galp_gb300.Graph(g.offsets, nbr), 3)
 
 
 def test_mid_degree_ties():
