@@ -29,7 +29,7 @@ ORACLE = os.path.join(ROOT, "oracle")
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CUDA_SOURCES = ["galp_capi.cu", "galp_tools.cu", "galp_noalloc.cu"]
+CUDA_SOURCES = ["galp_capi.cu", "galp_tools.cu", "galp_noalloc.cu", "galp_mlp.cu"]
 HOST_SOURCES = ["host/graph_io.cpp", "host/accuracy.cpp"]
 
 
@@ -61,11 +61,17 @@ def build(force: bool = False, verbose: bool = False) -> None:
     inc = os.path.join(ROOT, "include")
     jobs: list[tuple[str, list[str], list[str]]] = []
 
+    # CUDA sources compile to objects in parallel, then link into libgalp.so (second phase)
+    os.makedirs(os.path.join(LIB, "obj"), exist_ok=True)
     cuda_out = os.path.join(LIB, "libgalp.so")
     cuda_deps = _deps(CSRC, inc)
-    jobs.append((cuda_out, cuda_deps, [NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-                                       "-shared", "-o", cuda_out,
-                                       *[os.path.join(CSRC, s) for s in CUDA_SOURCES]]))
+    objs = []
+    for src in CUDA_SOURCES:
+        obj = os.path.join(LIB, "obj", src.replace(".cu", ".o"))
+        objs.append(obj)
+        jobs.append((obj, cuda_deps, [NVCC, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
+                                      "-o", obj, os.path.join(CSRC, src)]))
+    link_jobs = [(cuda_out, objs, [NVCC, *ARCH, "-shared", "-o", cuda_out, *objs])]
 
     gen_out = os.path.join(LIB, "libgalp_gen.so")
     gen_src = os.path.join(PKG, "gen", "generators.cpp")
@@ -80,9 +86,10 @@ def build(force: bool = False, verbose: bool = False) -> None:
         cli_src = os.path.join(PKG, "host", "main.cpp")
         cli_out = os.path.join(LIB, "galp")
         if os.path.exists(cli_src):
-            jobs.append((cli_out, [cli_src, *host_srcs, os.path.join(inc, "galp.h")],
-                         [NVCC, *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fopenmp", "-o", cli_out, cli_src,
-                          *host_srcs, *[os.path.join(CSRC, s) for s in CUDA_SOURCES], "-lgomp"]))
+            # the CLI links libgalp.so next to it (found through $ORIGIN)
+            link_jobs.append((cli_out, [cli_src, *host_srcs, os.path.join(inc, "galp.h"), cuda_out],
+                              ["g++", "-O2", "-std=c++17", "-fopenmp", "-o", cli_out, cli_src, *host_srcs,
+                               "-L" + LIB, "-lgalp", "-Wl,-rpath,$ORIGIN"]))
 
     orc_out = os.path.join(ORACLE, "_build", "liblp_oracle.so")
     orc_src = [os.path.join(ORACLE, "lp_oracle.c")]
@@ -93,9 +100,17 @@ def build(force: bool = False, verbose: bool = False) -> None:
         jobs.append((port_out, [port_src], ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-o",
                                             port_out, port_src]))
 
+    failed = _run_jobs(jobs, force, verbose, extra_ref=True)
+    if not failed:
+        failed = _run_jobs(link_jobs, force, verbose, extra_ref=False)
+    if failed:
+        raise RuntimeError("galp_gb300 build failed: " + ", ".join(failed))
+
+
+def _run_jobs(jobs, force: bool, verbose: bool, extra_ref: bool) -> list[str]:
     todo = [(o, cmd) for o, deps, cmd in jobs if force or not _newer(o, deps)]
     ref_script = os.path.join(ORACLE, "build_ref.sh")
-    ref_needed = os.path.isdir(os.environ.get("GALP_REFERENCE", "/root/reference")) and (
+    ref_needed = extra_ref and os.path.isdir(os.environ.get("GALP_REFERENCE", "/root/reference")) and (
         force or not _newer(os.path.join(ORACLE, "_ref", "ref_harness"), _deps(os.path.join(ORACLE, "refsim"))))
     with ThreadPoolExecutor(max_workers=max(1, len(todo) + 1)) as ex:
         futs = [ex.submit(_run, cmd) for _, cmd in todo]
@@ -108,8 +123,7 @@ def build(force: bool = False, verbose: bool = False) -> None:
                 sys.stderr.write(" ".join(cmd) + "\n" + out)
             if rc:
                 failed.append(cmd[-1])
-    if failed:
-        raise RuntimeError("galp_gb300 build failed: " + ", ".join(failed))
+    return failed
 
 
 if __name__ == "__main__":

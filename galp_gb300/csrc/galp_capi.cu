@@ -21,6 +21,7 @@
 #include "../../include/galp.h"
 #include "lp_kernels.cuh"
 #include "galp_ctx.h"
+#include "dispatch_weights.inc"
 #include "../../include/galp_tools.h"
 
 using namespace galp;
@@ -130,6 +131,13 @@ void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         sc.nml = (int32_t)large.size();
         S.mid_v.insert(S.mid_v.end(), xl.begin(), xl.end());
         sc.nmx = (int32_t)xl.size();
+        // the scope's mid list in ascending degree (stable): any degree threshold is a
+        // cut position, so the kernel split can change per iteration
+        std::stable_sort(S.mid_v.begin() + sc.m0, S.mid_v.end(), [off](int32_t x, int32_t y) {
+            return off[x + 1] - off[x] < off[y + 1] - off[y];
+        });
+        for (size_t i = (size_t)sc.m0; i < S.mid_v.size(); ++i)
+            S.mid_deg.push_back((int32_t)(off[S.mid_v[i] + 1] - off[S.mid_v[i]]));
         sc.np = (int32_t)S.pack_v0.size() - sc.p0;
         sc.nb = (int32_t)S.big_v.size() - sc.b0;
         sc.nc = (int32_t)S.chunk_big.size() - sc.c0;
@@ -260,10 +268,33 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     GALP_CUDA(b_tsmall.alloc(sizeof(int32_t) * (size_t)std::max<int64_t>(sched.max_scope_small, 1)));
     GALP_CUDA(b_tmid.alloc(sizeof(int32_t) * (size_t)std::max<int64_t>(sched.max_scope_mid, 1)));
     GALP_CUDA(b_bsum.alloc(sizeof(int64_t) * (size_t)std::max<int64_t>((sched.max_scope_vertices + kScanBlock - 1) / kScanBlock, 1)));
-    if (frontier) {
-        GALP_CUDA(b_dirty.alloc(nn));
-        GALP_CUDA(b_changed.alloc(sizeof(int32_t) * nn));
+    // dispatch: static features, variant table, per-scope state, logs
+    {
+        float sf[kDegBins + 3] = {};
+        for (int64_t v = 0; v < n; ++v) {
+            const int64_t d = g.offsets[v + 1] - g.offsets[v];
+            if (d <= 0) continue;
+            int b = 0;
+            while (b < kDegBins - 1 && (d >> (b + 1))) ++b;
+            sf[b] += (float)d;
+        }
+        for (int b = 0; b < kDegBins; ++b) sf[b] = m > 0 ? sf[b] / (float)m : 0.f;
+        sf[kDegBins] = (float)(std::log2((double)std::max<int64_t>(m, 1)) / 40.0);
+        sf[kDegBins + 1] = (float)(std::log2((double)std::max<int64_t>(n, 1)) / 40.0);
+        sf[kDegBins + 2] = (float)(std::log2(std::max(1.0, (double)m / (double)std::max<int64_t>(n, 1))) / 16.0);
+        GALP_CUDA(b_static_feat.alloc(sizeof(sf)));
+        GALP_CUDA(cudaMemcpyAsync(b_static_feat.p, sf, sizeof(sf), cudaMemcpyHostToDevice, st));
+        std::memcpy(static_feat, sf, sizeof(sf));
+        build_variant_table();
+        GALP_CUDA(b_vtab.alloc(sizeof(DispatchState) * kVar));
+        GALP_CUDA(cudaMemcpyAsync(b_vtab.p, vtab.data(), sizeof(DispatchState) * kVar, cudaMemcpyHostToDevice, st));
+        GALP_CUDA(b_disp.alloc(sizeof(DispatchState) * std::max<size_t>(sched.scopes.size(), 1)));
+        GALP_CUDA(b_feat_log.alloc(sizeof(float) * kMaxLogIters * kFeat));
+        GALP_CUDA(b_var_log.alloc(sizeof(int32_t) * kMaxLogIters));
+        GALP_CUDA(b_weights.alloc(sizeof(float) * mlp_param_count(kFeat, kHid, kVar)));
+        GALP_CUDA(cudaStreamSynchronize(st));
     }
+
     GALP_CUDA(b_lab0.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
     GALP_CUDA(b_lab1.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1)));
     GALP_CUDA(b_ctl.alloc(sizeof(Ctl)));
@@ -291,23 +322,32 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
         GALP_CUDA(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
         GALP_CUDA(cudaStreamSynchronize(st));
         if (bad) return GALP_EFORMAT;
-        // strictly increasing adjacency enables the first-iteration shortcut
-        GALP_CUDA(cudaMemsetAsync(b_bad.p, 0, sizeof(int), st));
-        adjacency_order_kernel<<<1024, 256, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p, n,
-                                                     (int *)b_bad.p);
+        // strictly increasing adjacency enables the first-iteration shortcut, a symmetric
+        // edge multiset the frontier
+        GALP_CUDA(b_chk.alloc(3 * sizeof(unsigned long long)));
+        GALP_CUDA(cudaMemsetAsync(b_chk.p, 0, 3 * sizeof(unsigned long long), st));
+        adjacency_check_kernel<<<1024, kTB, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p, n,
+                                                     (unsigned long long *)b_chk.p);
         GALP_CUDA(cudaGetLastError());
-        int unsorted = 0;
-        GALP_CUDA(cudaMemcpyAsync(&unsorted, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        unsigned long long chk[3] = {1, 1, 1};
+        GALP_CUDA(cudaMemcpyAsync(chk, b_chk.p, sizeof(chk), cudaMemcpyDeviceToHost, st));
         GALP_CUDA(cudaStreamSynchronize(st));
-        adj_sorted = unsorted == 0;
+        adj_sorted = chk[0] == 0;
+        symmetric = chk[1] == 0 && chk[2] == 0;
+        if (!symmetric) frontier = false;
+    }
+    if (frontier) {
+        GALP_CUDA(b_dirty.alloc(nn));
+        GALP_CUDA(b_changed.alloc(sizeof(int32_t) * nn));
     }
     GALP_CUDA(cudaStreamSynchronize(st));
 
     int dev = 0;
     GALP_CUDA(cudaGetDevice(&dev));
     GALP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    GALP_CUDA(cudaFuncSetAttribute(count_cta_kernel<512, kXlSlots>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(sizeof(uint32_t) * 2 * kXlSlots)));
+    GALP_CUDA(cudaFuncSetAttribute(count_cta_kernel<kXlThreads, kXlSlots>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(unsigned long long) * kXlSlots)));
     return GALP_OK;
 }
 
@@ -343,9 +383,45 @@ IterArgs Engine::big_args(const Scope &sc) const
     return a;
 }
 
+// Variant table rows of the in-core scope: k = 8 * aggregated + 4 * (warp/CTA split at
+// 128) + 2 * (CTA split at 1024) + frontier.  Row 0 is the fixed heuristic's dense
+// iteration and row 1 its frontier iteration.
+void Engine::build_variant_table()
+{
+    vtab.assign(kVar, DispatchState{});
+    const Scope &sc = sched.scopes.empty() ? Scope() : sched.scopes[0];
+    auto cut = [&](int t) {  // mid-list entries of degree <= t
+        const int32_t *b = sched.mid_deg.data() + sc.m0;
+        const int cnt = sc.nms + sc.nml + sc.nmx;
+        return (int32_t)(std::upper_bound(b, b + cnt, t) - b);
+    };
+    for (int k = 0; k < kVar; ++k) {
+        DispatchState &d = vtab[k];
+        d.agg_mode = (k & 8) ? 1 : 2;
+        d.pos1 = cut((k & 4) ? 128 : kMidSMax);
+        d.pos2 = cut((k & 2) ? 1024 : kLargeMax);
+        d.frontier = k & 1;
+        d.variant = k;
+    }
+}
+
+// Static per-scope states of the fixed rule (out-of-core scopes).
+std::vector<DispatchState> Engine::static_dispatch() const
+{
+    std::vector<DispatchState> ds(std::max<size_t>(sched.scopes.size(), 1));
+    for (size_t j = 0; j < sched.scopes.size(); ++j) {
+        const Scope &sc = sched.scopes[j];
+        ds[j].agg_mode = variant.agg_mode;
+        ds[j].pos1 = sc.nms;
+        ds[j].pos2 = sc.nms + sc.nml;
+    }
+    return ds;
+}
+
 PipeArgs Engine::pipe_args(const Scope &sc) const
 {
     PipeArgs q{};
+    q.disp = (const DispatchState *)b_disp.p + (&sc - sched.scopes.data());
     q.nbr_shift = (policy == 0) ? 0 : sc.e0;
     q.off = (const int64_t *)b_off.p;
     q.ctl = (Ctl *)b_ctl.p;
@@ -390,47 +466,67 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
     q.changed = changed;
     Ctl *ctl = (Ctl *)b_ctl.p;
     GALP_CUDA(cudaMemsetAsync(&ctl->tied_small, 0, 2 * sizeof(int), st));
+    prof.kmark("memset", st);
     int e0 = -1;
     if (a.nbig) {
         if (prof.on) e0 = prof.mark(st);
         big_insert_kernel<<<a.nchunks, kTB, 0, st>>>(a);
-        for (int pass = 0; pass < 3; ++pass) big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a, pass);
+        launched("big_insert_kernel", st);
+        for (int pass = 0; pass < 3; ++pass) {
+            big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a, pass);
+            launched("big_stats_kernel", st);
+        }
         big_dcnt_kernel<<<(a.nbig + 255) / 256, 256, 0, st>>>(a, q.dcnt);
+        launched("big_dcnt_kernel", st);
         if (prof.on) prof.spans[1].push_back({e0, prof.mark(st)});
     }
     if (prof.on) e0 = prof.mark(st);
     if (q.npacks) {
         const int blocks = (int)std::min<int64_t>(((int64_t)q.npacks * 32 + 255) / 256, (int64_t)sms * 16);
         count_small_kernel<<<blocks, 256, 0, st>>>(q);
+        launched("count_small_kernel", st);
     }
-    if (q.nmid_s) {
-        const int blocks = (int)std::min<int64_t>((q.nmid_s + kMidWarps - 1) / kMidWarps, (int64_t)sms * 6);
-        count_mid_kernel<<<blocks, 32 * kMidWarps, 0, st>>>(q);
-    }
-    if (q.nmid_l) {
-        const int blocks = (int)std::min<int64_t>(q.nmid_l, (int64_t)sms * 6);
-        count_cta_kernel<kTB, 2 * kLargeMax><<<blocks, kTB, sizeof(uint32_t) * 4 * kLargeMax, st>>>(q, q.nmid_s, q.nmid_l);
-    }
-    if (q.nmid_x) {
-        const int blocks = (int)std::min<int64_t>(q.nmid_x, (int64_t)sms);
-        count_cta_kernel<512, kXlSlots><<<blocks, 512, sizeof(uint32_t) * 2 * kXlSlots, st>>>(q, q.nmid_s + q.nmid_l,
-                                                                                            q.nmid_x);
+    if (q.nmid_s + q.nmid_l + q.nmid_x) {
+        // ranges of the degree-sorted mid list come from the dispatch state
+        count_mid_kernel<<<(int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1, (int64_t)sms * 6),
+                           32 * kMidWarps, 0, st>>>(q);
+        launched("count_mid_kernel", st);
+        count_cta_kernel<kTB, 2 * kLargeMax>
+            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 6)), kTB,
+               sizeof(unsigned long long) * 2 * kLargeMax, st>>>(q, 0);
+        launched("count_cta_kernel<large>", st);
+        if (q.nmid_x) {
+            count_cta_kernel<kXlThreads, kXlSlots>
+                <<<(int)std::min<int64_t>(q.nmid_x, (int64_t)sms), kXlThreads, sizeof(unsigned long long) * kXlSlots,
+                   st>>>(q, 1);
+            launched("count_cta_kernel<xl>", st);
+        }
     }
     const int64_t nv = sc.v1 - sc.v0;
     if (nv > 0) {
         const int nblk = (int)((nv + kScanBlock - 1) / kScanBlock);
         scan_reduce_kernel<<<nblk, kTB, 0, st>>>(q);
+        launched("scan_reduce_kernel", st);
         scan_spine_kernel<<<1, kTB, 0, st>>>(q, nblk);
+        launched("scan_spine_kernel", st);
         scan_apply_kernel<<<nblk, kTB, 0, st>>>(q);
+        launched("scan_apply_kernel", st);
     }
     resolve_small_kernel<<<sms * 4, kTB, 0, st>>>(q);
-    if (q.nmid_s + q.nmid_l + q.nmid_x) resolve_mid_kernel<<<sms * 2, kTB, 0, st>>>(q);
+    launched("resolve_small_kernel", st);
+    if (q.nmid_s + q.nmid_l + q.nmid_x) {
+        resolve_mid_kernel<<<sms * 2, kTB, 0, st>>>(q);
+        launched("resolve_mid_kernel", st);
+    }
     if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
     if (a.nbig) {
         if (prof.on) e0 = prof.mark(st);
         big_resolve_kernel<<<a.nbig, 32, sizeof(uint32_t) * kPickScratch, st>>>(a);
+        launched("big_resolve_kernel", st);
         big_clear_kernel<<<a.nschunks, kTB, 0, st>>>(a);
+        launched("big_clear_kernel", st);
         big_reset_kernel<<<(a.nbig + 255) / 256, 256, 0, st>>>(a);
+        launched("big_reset_kernel", st);
         if (prof.on) prof.spans[2].push_back({e0, prof.mark(st)});
     }
     GALP_CUDA(cudaGetLastError());
@@ -439,13 +535,40 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
 
 int Engine::enqueue_init(cudaStream_t st, int niter, long long thr)
 {
+    prof.kstart(st);
     if (n > 0) {
         const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
         init_labels_kernel<<<blocks, 256, 0, st>>>((int32_t *)b_lab0.p, n);
+        launched("init_labels_kernel", st);
     }
     init_ctl_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p, thr, niter);
+    launched("init_ctl_kernel", st);
     GALP_CUDA(cudaGetLastError());
     return GALP_OK;
+}
+
+DispatchArgs Engine::dispatch_args(int it) const
+{
+    DispatchArgs a{};
+    a.ctl = (const Ctl *)b_ctl.p;
+    a.table = (const DispatchState *)b_vtab.p;
+    a.weights = (const float *)b_weights.p;
+    a.static_feat = (const float *)b_static_feat.p;
+    a.out = (DispatchState *)b_disp.p;
+    a.feat_log = (float *)b_feat_log.p;
+    a.var_log = (int32_t *)b_var_log.p;
+    a.n = n;
+    a.m = m;
+    a.it = it;
+    a.mode = disp_mode;
+    a.forced = disp_forced;
+    a.frontier_mode = frontier ? 1 : 0;
+    a.frontier_frac = variant.frontier_frac;
+    a.fixed_variant_dense = 0;
+    a.fixed_variant_front = 1;
+    a.fixed_agg = variant.agg_mode;
+    a.margin = variant.learned_margin;
+    return a;
 }
 
 int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
@@ -453,23 +576,35 @@ int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
     int32_t *lab[2] = {(int32_t *)b_lab0.p, (int32_t *)b_lab1.p};
     int rc = enqueue_init(st, niter, thr);
     if (rc) return rc;
+    GALP_CUDA(cudaMemsetAsync(b_var_log.p, 0xFF, sizeof(int32_t) * kMaxLogIters, st));
+    GALP_CUDA(cudaMemsetAsync(b_feat_log.p, 0, sizeof(float) * kMaxLogIters * kFeat, st));
     Ctl *ctl = (Ctl *)b_ctl.p;
     uint8_t *dirty = frontier ? (uint8_t *)b_dirty.p : nullptr;
     int32_t *changed = frontier ? (int32_t *)b_changed.p : nullptr;
     bool full_state = false;  // per-vertex counts and summaries hold the previous iteration
     for (int it = 0; it < niter; ++it) {
+        const int it0 = prof.on ? prof.mark(st) : -1;
+        const bool shortcut = it == 0 && adj_sorted && n > 0;
+        if (!shortcut) {
+            // this iteration's kernel variant, decided on the device
+            dispatch_kernel<<<1, kHid, 0, st>>>(dispatch_args(it));
+            launched("dispatch_kernel", st);
+        }
         const uint8_t *dirty_it = nullptr;
         if (frontier) {
             if (full_state) {
                 // vertices next to a label that changed in the previous iteration
                 GALP_CUDA(cudaMemsetAsync(dirty, 0, (size_t)n, st));
+                prof.kmark("memset", st);
                 mark_dirty_kernel<<<sms * 8, kTB, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p,
-                                                           changed, (int)n, ctl, dirty);
+                                                           changed, (const DispatchState *)b_disp.p, ctl, dirty);
+                launched("mark_dirty_kernel", st);
                 dirty_it = dirty;
             }
             GALP_CUDA(cudaMemsetAsync(&ctl->changed_n, 0, sizeof(int), st));
+            prof.kmark("memset", st);
         }
-        if (it == 0 && adj_sorted && n > 0) {
+        if (shortcut) {
             PipeArgs q = pipe_args(sched.scopes[0]);
             q.nbr = (const int32_t *)b_nbr[0].p;
             q.lab_in = lab[0];
@@ -477,6 +612,7 @@ int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
             q.changed = changed;
             int e0 = prof.on ? prof.mark(st) : -1;
             first_iteration_kernel<<<(int)std::min<int64_t>((n + kTB - 1) / kTB, (int64_t)sms * 8), kTB, 0, st>>>(q, n, m);
+            launched("first_iteration_kernel", st);
             if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
             full_state = false;  // the shortcut leaves no per-vertex counts behind
         } else {
@@ -486,6 +622,8 @@ int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
             full_state = true;
         }
         finalize_kernel<<<1, 1, 0, st>>>(ctl);
+        launched("finalize_kernel", st);
+        if (prof.on) prof.it_spans.push_back({it0, prof.mark(st)});
     }
     GALP_CUDA(cudaGetLastError());
     return GALP_OK;
@@ -501,6 +639,9 @@ int Engine::run_outofcore(cudaStream_t st, int niter, long long thr)
     int32_t *cur = (int32_t *)b_lab0.p, *tmp = (int32_t *)b_lab1.p;
     int rc = enqueue_init(st, niter, thr);
     if (rc) return rc;
+    const std::vector<DispatchState> ds = static_dispatch();
+    GALP_CUDA(cudaMemcpyAsync(b_disp.p, ds.data(), sizeof(DispatchState) * ds.size(), cudaMemcpyHostToDevice, st));
+    GALP_CUDA(cudaStreamSynchronize(st));  // ds is a local
     h2d_run = 0;
     const int nb = (int)sched.scopes.size();
     auto copy_batch = [&](int j, int buf, cudaStream_t s) -> int {
@@ -533,6 +674,7 @@ int Engine::run_outofcore(cudaStream_t st, int niter, long long thr)
             const int32_t *nbr = (const int32_t *)b_nbr[buf].p;
             if (it == 0 && sc.e1 > sc.e0) {
                 validate_batch_kernel<<<256, 256, 0, st>>>(nbr, sc.e1 - sc.e0, n, (Ctl *)b_ctl.p);
+                launched("validate_batch_kernel", st);
                 GALP_CUDA(cudaGetLastError());
             }
             if ((rc = enqueue_scope(st, sc, nbr, cur, tmp))) return rc;
@@ -542,6 +684,7 @@ int Engine::run_outofcore(cudaStream_t st, int niter, long long thr)
             if (policy == 2) GALP_CUDA(cudaEventRecord(ev_consumed[buf], st));
         }
         finalize_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p);
+        launched("finalize_kernel", st);
         GALP_CUDA(cudaGetLastError());
         int active = 0;
         GALP_CUDA(cudaMemcpyAsync(&active, &((Ctl *)b_ctl.p)->active, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -621,6 +764,17 @@ int galp_create(const galp_csr *g, const galp_opts *o, galp_ctx **out)
     ctx->stream = ctx->own_stream;
     int rc = ctx->eng.setup(*g, opts, ctx->stream, ctx->h2d_setup);
     if (rc) return rc;
+    if (opts.dispatch == 1) {  // the built-in trained dispatcher
+#if GALP_HAVE_TRAINED_DISPATCH
+        rc = galp_dispatch_set(ctx.get(), 1, 0, kTrainedDispatch,
+                               (int64_t)(sizeof(kTrainedDispatch) / sizeof(kTrainedDispatch[0])));
+        if (rc) return rc;
+#else
+        return GALP_EUNSUPPORTED;
+#endif
+    } else if (opts.dispatch != 0) {
+        return GALP_EINVAL;
+    }
     GALP_CUDA(cudaEventCreate(&ctx->ev0));
     GALP_CUDA(cudaEventCreate(&ctx->ev1));
     ctx->t_pre = now_s() - t0;
@@ -742,20 +896,99 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
     int64_t nms = 0, nml = 0;
     for (const galp::Scope &sc : E.sched.scopes) {
         nms += sc.nms;
-        nml += sc.nml;
+        nml += sc.nml + sc.nmx;
     }
     info->nmid = nms;
     info->nlarge = nml;
     info->nbig = (int64_t)E.sched.big_v.size();
     info->table_slots = E.sched.max_table_slots;
-    info->launches_per_iter = 9 + (info->nbig ? 8 : 0);
+    info->launches_per_iter = 10 + (info->nbig ? 8 : 0) + (E.frontier ? 1 : 0);
+    info->flags = (E.adj_sorted ? GALP_SCHED_SORTED : 0) | (E.symmetric ? GALP_SCHED_SYMMETRIC : 0) |
+                  (E.frontier ? GALP_SCHED_FRONTIER : 0);
+    info->launches = E.launches;
     return GALP_OK;
 }
 
-int galp_profile(galp_ctx *ctx, int32_t enable)
+int galp_set_variant(galp_ctx *ctx, const galp_variant *v)
 {
-    if (!ctx) return GALP_EINVAL;
-    ctx->eng.prof.on = enable != 0;
+    if (!ctx || !v || v->agg_mode < 0 || v->agg_mode > 2 || !(v->frontier_frac >= 0.f && v->frontier_frac <= 1.f) ||
+        !(v->learned_margin >= 0.f && v->learned_margin < 10.f))
+        return GALP_EINVAL;
+    ctx->eng.variant = *v;
+    return GALP_OK;
+}
+
+int galp_get_variant(galp_ctx *ctx, galp_variant *v)
+{
+    if (!ctx || !v) return GALP_EINVAL;
+    *v = ctx->eng.variant;
+    return GALP_OK;
+}
+
+int galp_dispatch_set(galp_ctx *ctx, int32_t mode, int32_t forced_variant, const float *weights, int64_t count)
+{
+    if (!ctx || mode < 0 || mode > 2) return GALP_EINVAL;
+    galp::Engine &E = ctx->eng;
+    if (mode == 2 && (forced_variant < 0 || forced_variant >= galp::kVar)) return GALP_EINVAL;
+    if (weights) {
+        if (count != galp::mlp_param_count(galp::kFeat, galp::kHid, galp::kVar)) return GALP_EINVAL;
+        GALP_CUDA(cudaMemcpyAsync(E.b_weights.p, weights, sizeof(float) * count, cudaMemcpyHostToDevice, ctx->stream));
+        GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+        E.have_weights = true;
+    }
+    if (mode == 1 && !E.have_weights) return GALP_EINVAL;
+    E.disp_mode = mode;
+    E.disp_forced = forced_variant;
+    return GALP_OK;
+}
+
+int galp_dispatch_log(galp_ctx *ctx, float *features, int32_t *variants, int32_t cap_iters, int32_t *count)
+{
+    if (!ctx || !count || cap_iters < 0) return GALP_EINVAL;
+    galp::Engine &E = ctx->eng;
+    GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int nlog = std::min(std::min(ctx->iters, (int)galp::kMaxLogIters), (int)cap_iters);
+    *count = nlog;
+    if (nlog > 0 && features)
+        GALP_CUDA(cudaMemcpy(features, E.b_feat_log.p, sizeof(float) * galp::kFeat * nlog, cudaMemcpyDeviceToHost));
+    if (nlog > 0 && variants)
+        GALP_CUDA(cudaMemcpy(variants, E.b_var_log.p, sizeof(int32_t) * nlog, cudaMemcpyDeviceToHost));
+    return GALP_OK;
+}
+
+int galp_dispatch_table(galp_ctx *ctx, galp_dispatch_row *rows, int32_t cap, int32_t *count)
+{
+    if (!ctx || !count || cap < 0 || (cap > 0 && !rows)) return GALP_EINVAL;
+    const galp::Engine &E = ctx->eng;
+    *count = (int32_t)E.vtab.size();
+    for (int32_t k = 0; k < cap && k < *count; ++k) {
+        rows[k].agg_mode = E.vtab[k].agg_mode;
+        rows[k].frontier = E.vtab[k].frontier;
+        rows[k].warp_max_degree = (k & 4) ? 128 : galp::kMidSMax;
+        rows[k].cta256_max_degree = (k & 2) ? 1024 : galp::kLargeMax;
+        rows[k].pos1 = E.vtab[k].pos1;
+        rows[k].pos2 = E.vtab[k].pos2;
+    }
+    return GALP_OK;
+}
+
+int galp_profile_iterations(galp_ctx *ctx, float *ms, int32_t cap, int32_t *count)
+{
+    if (!ctx || !count || cap < 0 || (cap > 0 && !ms)) return GALP_EINVAL;
+    GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+    galp::Profiler &P = ctx->eng.prof;
+    P.fold();
+    *count = (int32_t)P.it_ms.size();
+    for (int32_t i = 0; i < cap && i < *count; ++i) ms[i] = P.it_ms[i];
+    P.it_ms.clear();
+    return GALP_OK;
+}
+
+int galp_profile(galp_ctx *ctx, int32_t level)
+{
+    if (!ctx || level < 0 || level > 2) return GALP_EINVAL;
+    ctx->eng.prof.level = level;
+    ctx->eng.prof.on = level >= 1;
     return GALP_OK;
 }
 
@@ -765,17 +998,34 @@ int galp_profile_read(galp_ctx *ctx, galp_kernel_times *out)
     std::memset(out, 0, sizeof(*out));
     GALP_CUDA(cudaStreamSynchronize(ctx->stream));
     galp::Profiler &P = ctx->eng.prof;
-    double *ms[3] = {&out->pipe_ms, &out->big_pre_ms, &out->big_post_ms};
-    int32_t *cnt[3] = {&out->pipe_groups, &out->big_pre_groups, &out->big_post_groups};
+    P.fold();
+    out->pipe_ms = P.group_ms[0];
+    out->pipe_groups = P.group_n[0];
+    out->big_pre_ms = P.group_ms[1];
+    out->big_pre_groups = P.group_n[1];
+    out->big_post_ms = P.group_ms[2];
+    out->big_post_groups = P.group_n[2];
     for (int g = 0; g < 3; ++g) {
-        for (auto &sp : P.spans[g]) {
-            float t = 0.f;
-            if (cudaEventElapsedTime(&t, P.pool[sp.first], P.pool[sp.second]) == cudaSuccess) *ms[g] += t;
-            ++*cnt[g];
-        }
-        P.spans[g].clear();
+        P.group_ms[g] = 0;
+        P.group_n[g] = 0;
     }
-    P.used = 0;
+    return GALP_OK;
+}
+
+int galp_profile_kernels(galp_ctx *ctx, galp_kernel_stat *out, int32_t cap, int32_t *count)
+{
+    if (!ctx || !count || cap < 0 || (cap > 0 && !out)) return GALP_EINVAL;
+    GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+    galp::Profiler &P = ctx->eng.prof;
+    P.fold();
+    *count = (int32_t)P.kstats.size();
+    for (int32_t i = 0; i < cap && i < *count; ++i) {
+        std::memset(&out[i], 0, sizeof(out[i]));
+        std::strncpy(out[i].name, P.kstats[i].first, sizeof(out[i].name) - 1);
+        out[i].ms = P.kstats[i].second.first;
+        out[i].launches = P.kstats[i].second.second;
+    }
+    P.kstats.clear();
     return GALP_OK;
 }
 

@@ -4,9 +4,11 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "../../include/galp.h"
+#include "../../include/galp_tools.h"
 #include "lp_pipeline.cuh"
 
 namespace galp {
@@ -60,7 +62,8 @@ struct Scope {
 struct Schedule {
     std::vector<int32_t> pack_v0;    // first vertex of each pack (<= 32 vertices, <= 32 edges)
     std::vector<uint8_t> pack_nv;    // vertices in each pack
-    std::vector<int32_t> mid_v;      // per scope: mid vertices, then large vertices
+    std::vector<int32_t> mid_v;      // per scope: mid, large and xl vertices in ascending degree
+    std::vector<int32_t> mid_deg;    // degree of each mid_v entry
     std::vector<int32_t> big_v;      // vertex of each big entry
     std::vector<int64_t> big_toff;   // table offset, relative to its scope
     std::vector<uint32_t> big_tcap;  // table capacity (power of two >= 2 * degree)
@@ -81,12 +84,21 @@ void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
 // 2^buffer_pow edges; returns GALP_EBATCH where the reference would loop forever.
 int batch_boundaries(int64_t n, const int64_t *off, int buffer_pow, std::vector<int64_t> &bbs);
 
-// CUDA events around kernel groups (enabled by galp_profile).
+// CUDA events around kernel groups (level 1) and around every kernel (level 2), enabled
+// by galp_profile.  Intervals are folded into per-group and per-kernel-name totals.
 struct Profiler {
-    bool on = false;
+    bool on = false;  // level >= 1
+    int level = 0;
     std::vector<cudaEvent_t> pool;
     size_t used = 0;
     std::vector<std::pair<int, int>> spans[3];  // 0 = count/scan/resolve, 1 = big pre, 2 = big post
+    int last = -1;                              // level 2: mark that the next interval starts at
+    std::vector<std::pair<const char *, std::pair<int, int>>> kspans;
+    double group_ms[3] = {0, 0, 0};
+    int group_n[3] = {0, 0, 0};
+    std::vector<std::pair<const char *, std::pair<double, int64_t>>> kstats;  // name -> (ms, launches)
+    std::vector<std::pair<int, int>> it_spans;  // in-core iterations
+    std::vector<float> it_ms;
     int mark(cudaStream_t st)
     {
         if (used == pool.size()) {
@@ -96,6 +108,55 @@ struct Profiler {
         }
         cudaEventRecord(pool[used], st);
         return (int)used++;
+    }
+    void kstart(cudaStream_t st)
+    {
+        if (level >= 2) last = mark(st);
+    }
+    // level 2: close the interval since the previous mark under `name`
+    void kmark(const char *name, cudaStream_t st)
+    {
+        if (level < 2) return;
+        const int e = mark(st);
+        if (last >= 0 && e >= 0) kspans.push_back({name, {last, e}});
+        last = e;
+    }
+    // wait for the recorded events and fold their intervals into the totals
+    void fold()
+    {
+        for (int g = 0; g < 3; ++g) {
+            for (auto &sp : spans[g]) {
+                float t = 0.f;
+                if (sp.first >= 0 && sp.second >= 0 &&
+                    cudaEventSynchronize(pool[sp.second]) == cudaSuccess &&
+                    cudaEventElapsedTime(&t, pool[sp.first], pool[sp.second]) == cudaSuccess)
+                    group_ms[g] += t;
+                ++group_n[g];
+            }
+            spans[g].clear();
+        }
+        for (auto &ks : kspans) {
+            float t = 0.f;
+            if (cudaEventSynchronize(pool[ks.second.second]) != cudaSuccess ||
+                cudaEventElapsedTime(&t, pool[ks.second.first], pool[ks.second.second]) != cudaSuccess)
+                t = 0.f;
+            size_t i = 0;
+            while (i < kstats.size() && std::strcmp(kstats[i].first, ks.first) != 0) ++i;
+            if (i == kstats.size()) kstats.push_back({ks.first, {0.0, 0}});
+            kstats[i].second.first += t;
+            kstats[i].second.second += 1;
+        }
+        kspans.clear();
+        for (auto &sp : it_spans) {
+            float t = 0.f;
+            if (sp.first < 0 || sp.second < 0 || cudaEventSynchronize(pool[sp.second]) != cudaSuccess ||
+                cudaEventElapsedTime(&t, pool[sp.first], pool[sp.second]) != cudaSuccess)
+                t = -1.f;
+            it_ms.push_back(t);
+        }
+        it_spans.clear();
+        used = 0;
+        last = -1;
     }
     ~Profiler()
     {
@@ -114,8 +175,14 @@ struct Engine {
     DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff;
     DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_gkey, b_gcnt, b_occ, b_bad;
     DevBuf b_dcnt, b_runbase, b_c0, b_c1, b_kw, b_r, b_run_lab, b_run_cnt, b_tsmall, b_tmid, b_bsum;
-    DevBuf b_dirty, b_changed;  // frontier mode
-    bool frontier = false;
+    DevBuf b_dirty, b_changed, b_chk;  // frontier mode; setup adjacency checks
+    DevBuf b_static_feat, b_vtab, b_disp, b_feat_log, b_var_log, b_weights;  // dispatch
+    float static_feat[kDegBins + 3] = {};
+    std::vector<DispatchState> vtab;   // variant table of the in-core scope
+    int disp_mode = 0;                 // 0 fixed rule, 1 learned MLP, 2 forced variant
+    int disp_forced = 0;
+    bool have_weights = false;
+    bool frontier = false;             // requested, policy 0, and the graph is symmetric
     int32_t *d_pack_v0 = nullptr;
     uint8_t *d_pack_nv = nullptr;
     int32_t *d_mid_v = nullptr;
@@ -128,17 +195,28 @@ struct Engine {
     int64_t *d_schunk_s0 = nullptr, *d_schunk_s1 = nullptr;
     int sms = 1;
     bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
+    bool symmetric = false;   // edge multiset symmetric (frontier marking along out-edges)
     Profiler prof;
+    galp_variant variant{2, 0.05f, 0.03f, {}};  // kernel variant knobs (galp_set_variant)
     // out-of-core streaming
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     uint64_t batch_seq = 0;   // running batch counter (buffer parity)
     int64_t h2d_run = 0;      // bytes streamed by the last run
+    int64_t launches = 0;     // kernels launched by runs so far (setup excluded)
+    void launched(const char *name, cudaStream_t st)
+    {
+        ++launches;
+        prof.kmark(name, st);
+    }
 
     ~Engine();
     int setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_t &h2d);
     IterArgs big_args(const Scope &sc) const;
     PipeArgs pipe_args(const Scope &sc) const;
+    void build_variant_table();
+    std::vector<DispatchState> static_dispatch() const;
+    DispatchArgs dispatch_args(int it) const;
     int enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
                       int32_t *lab_out, const uint8_t *dirty = nullptr, int32_t *changed = nullptr);
     int enqueue_run_incore(cudaStream_t st, int niter, long long thr);

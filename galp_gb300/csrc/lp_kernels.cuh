@@ -58,7 +58,7 @@ struct Ctl {
     int tied_small;             // tied vertices listed by the count kernels (per scope)
     int tied_mid;
     int changed_n;              // vertices whose label changed (frontier mode)
-    int pad2;
+    int frontier_off;           // frontier mode: this iteration recounts every vertex
 };
 
 // Per-big-vertex statistics (reset by big_resolve after use).
@@ -1192,6 +1192,8 @@ __global__ void init_ctl_kernel(Ctl *ctl, long long thr, int max_iter)
     ctl->N = 0;
     ctl->thr = thr;
     ctl->max_iter = max_iter;
+    ctl->changed_n = 0;
+    ctl->frontier_off = 0;
     for (int i = 0; i < 64; ++i) ctl->counts[i] = 0;
 }
 

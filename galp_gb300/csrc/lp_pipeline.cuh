@@ -26,7 +26,9 @@
 //   occupied entries unsorted (queried by order statistics).
 #pragma once
 
+#include "rmat_rng.h"
 #include "lp_kernels.cuh"
+#include "lp_dispatch.cuh"
 
 namespace galp {
 
@@ -35,8 +37,9 @@ constexpr int kMidSCap = 2 * kMidSMax;
 constexpr int kMidWarps = 8;         // warps (vertices) per mid CTA
 constexpr int kScanBlock = 4096;     // vertices per scan block (256 threads x 16)
 constexpr int kLargeMax = 2048;      // large bucket: 257..2048, one 256-thread CTA each
-constexpr int kXlMax = 12288;        // xl bucket: 2049..12288, one 512-thread CTA each
-constexpr int kXlSlots = 2 * kXlMax; // 192 KB of shared-memory table
+constexpr int kXlMax = 12288;        // xl bucket: 2049..12288, one 1024-thread CTA each
+constexpr int kXlSlots = 2 * kXlMax; // 192 KB of shared-memory table (64-bit slots)
+constexpr int kXlThreads = 1024;
 
 struct PipeArgs {
     const int32_t *nbr;     // neighbour buffer holding CSR entries [nbr_shift, ...)
@@ -70,11 +73,18 @@ struct PipeArgs {
     // frontier mode (null = every vertex is recounted and no changes are recorded)
     const uint8_t *dirty;   // 1 = a neighbour's label changed in the previous iteration
     int32_t *changed;       // vertices whose label changes in this iteration
+    const DispatchState *disp;  // this iteration's variant (mid-list split, inserts, frontier)
 };
 
 __device__ __forceinline__ void count_change(unsigned long long &changes, int32_t nl, int32_t old)
 {
     changes += (nl != old);
+}
+
+// Frontier mode and this iteration not switched to a full recount.
+__device__ __forceinline__ bool frontier_on(const PipeArgs &p)
+{
+    return p.dirty && !*((volatile int *)&p.ctl->frontier_off);
 }
 
 // Record a changed vertex for the next iteration's frontier (single thread).
@@ -115,6 +125,7 @@ __device__ __forceinline__ void warp_note_changes(const PipeArgs &p, bool change
 __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
 {
     if (!ctl_active(p.ctl)) return;
+    const bool fr = frontier_on(p);
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -124,7 +135,7 @@ __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
         // vertex lanes: offsets, degrees, slot positions
         const bool vl = lane < nv;
         const int v = v0 + lane;
-        if (p.dirty && !__any_sync(kFull, vl && p.dirty[v])) {
+        if (fr && !__any_sync(kFull, vl && p.dirty[v])) {
             // no label around this pack changed: counts and summaries carry over; labels
             // of untied vertices stay, tied vertices are resolved again (run bases move)
             bool tied = false;
@@ -159,11 +170,11 @@ __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
         const int pj = __shfl_sync(kFull, pos, j);
         int lab = 0;
         if (valid) lab = __ldg(&p.lab_in[__ldg(&p.nbr[oj + (lane - pj) - p.nbr_shift])]);
-        // count in registers: segments of lanes per vertex
-        const unsigned long long key =
-            valid ? (((unsigned long long)(unsigned)j << 32) | (unsigned)lab) : (0xFFFFFFFF00000000ull | (unsigned)lane);
-        const unsigned eq = __match_any_sync(kFull, key);
-        const unsigned vm = __match_any_sync(kFull, valid ? j : (-1 - lane));
+        // count in registers: the slot lanes of vertex j are [pj, pj + deg_j)
+        const int dj = __shfl_sync(kFull, deg, j);
+        const unsigned vm = valid ? (((pj + dj >= 32) ? kFull : ((1u << (pj + dj)) - 1)) & ~((1u << pj) - 1))
+                                  : (1u << lane);
+        const unsigned eq = __match_any_sync(kFull, valid ? (uint32_t)lab : (0x80000000u | (uint32_t)lane)) & vm;
         const int cnt = __popc(eq);
         const bool leader = valid && ((__ffs(eq) - 1) == lane);
         const unsigned lm = __ballot_sync(kFull, leader);
@@ -178,39 +189,40 @@ __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
             const unsigned m = cm & vm;
             cmin = cmax = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : lane);
         } else {
-            // sort the pack by (vertex, label): runs become adjacent and ascending
-            unsigned long long sk = key;
-            int sc = valid ? cnt : 0;
+            cmin = seg_min(cand ? lab : INT_MAX, lane, first, last);
+            cmax = seg_max(cand ? lab : -1, lane, first, last);
+            rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
+            rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
+            if (__any_sync(kFull, valid && k > 2)) {
+                // resolving a vertex with more than two candidates may need its runs in
+                // label order: sort the pack by (vertex, label) and spill those runs
+                unsigned long long sk =
+                    valid ? (((unsigned long long)(unsigned)j << 32) | (unsigned)lab) : (0xFFFFFFFF00000000ull | lane);
+                int sc = valid ? cnt : 0;
 #pragma unroll
-            for (int kk = 2; kk <= 32; kk <<= 1) {
+                for (int kk = 2; kk <= 32; kk <<= 1) {
 #pragma unroll
-                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-                    const unsigned long long ok = __shfl_xor_sync(kFull, sk, jj);
-                    const int oc = __shfl_xor_sync(kFull, sc, jj);
-                    const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
-                    if ((lower == up) ? (ok < sk) : (ok > sk)) {
-                        sk = ok;
-                        sc = oc;
+                    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                        const unsigned long long ok = __shfl_xor_sync(kFull, sk, jj);
+                        const int oc = __shfl_xor_sync(kFull, sc, jj);
+                        const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
+                        if ((lower == up) ? (ok < sk) : (ok > sk)) {
+                            sk = ok;
+                            sc = oc;
+                        }
                     }
                 }
+                const int slab = (int)(unsigned)sk;
+                const int prev = __shfl_up_sync(kFull, slab, 1);
+                const bool head = valid && (lane == first || prev != slab);
+                const unsigned hm = __ballot_sync(kFull, head) & vm;
+                const int rank = __popc(hm & ((1u << lane) - 1));
+                if (head && k > 2) {
+                    const int64_t e = oj - p.nbr_shift + rank;
+                    p.run_lab[e] = slab;
+                    p.run_cnt[e] = (uint16_t)sc;
+                }
             }
-            const int slab = (int)(unsigned)sk;
-            const int prev = __shfl_up_sync(kFull, slab, 1);
-            const bool head = valid && (lane == first || prev != slab);
-            const unsigned hm = __ballot_sync(kFull, head) & vm;
-            const int rank = __popc(hm & ((1u << lane) - 1));
-            const unsigned cr = __ballot_sync(kFull, head && sc == W) & vm;
-            const bool tied_v = __popc(cr) > 1;
-            if (head && tied_v) {  // spill the sorted runs of tied vertices
-                const int64_t e = oj - p.nbr_shift + rank;
-                p.run_lab[e] = slab;
-                p.run_cnt[e] = (uint16_t)sc;
-            }
-            const int lo = cr ? (__ffs(cr) - 1) : lane, hi = cr ? (31 - __clz(cr)) : lane;
-            cmin = __shfl_sync(kFull, slab, lo);
-            cmax = __shfl_sync(kFull, slab, hi);
-            rmin = __popc(hm & ((1u << lo) - 1));
-            rmax = __popc(hm & ((1u << hi) - 1));
         }
         // results live at each vertex's first slot lane; bring them to the vertex lanes
         const int src = (vl && deg > 0) ? pos : lane;
@@ -245,107 +257,199 @@ __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
 }
 
 // ---------------------------------------------------------------------------
-// mid and large vertices: hash region in shared memory
+// mid, large and xl vertices: generation-tagged hash tables in shared memory
 // ---------------------------------------------------------------------------
+//
+// A slot is one 64-bit word: generation (19 bits) | label (31 bits) | count (14 bits).
+// Every vertex a table serves gets a new generation, so slots left by earlier vertices
+// read as free and the table is never cleared between vertices; an insert either adds
+// to the slot holding its label or claims a stale slot with one compare-and-swap.
+// Degrees stay below 2^14 on these paths and labels below 2^31.
+constexpr int kT64GenShift = 45;
+constexpr uint32_t kT64GenMax = (1u << 19) - 1;
+constexpr unsigned long long kT64CntMask = (1ull << 14) - 1;
 
-// Summary of one vertex's table region, computed by a group of threads.  `red` is a
-// reduction helper over the group.
-template <class Red>
-__device__ void table_summary(const uint32_t *key, const uint32_t *cnt, int cap, int gtid, int gsize, Red red,
-                              int &d, int &W, int &k, int &cmin, int &cmax, int &rmin, int &rmax)
+__device__ __forceinline__ unsigned long long t64_tag(uint32_t gen, uint32_t label)
 {
-    int dp = 0, wp = 0;
-    for (int s = gtid; s < cap; s += gsize)
-        if (key[s] != kEmpty) {
-            dp++;
-            wp = max(wp, (int)cnt[s]);
+    return ((unsigned long long)gen << kT64GenShift) | ((unsigned long long)label << 14);
+}
+
+// Returns the slot index when this insert claimed a new slot, else -1.
+__device__ __forceinline__ int t64_insert(unsigned long long *tab, uint32_t cap, uint32_t gen, uint32_t label,
+                                          uint32_t c)
+{
+    const unsigned long long tag = t64_tag(gen, label);
+    uint32_t h = hslot(label, cap);
+    unsigned long long cur = *(volatile unsigned long long *)&tab[h];
+    for (;;) {
+        if ((cur & ~kT64CntMask) == tag) {
+            // the count is the low 14 bits of the low word (little-endian), and the total
+            // stays below 2^14: a 32-bit add never carries into the label
+            atomicAdd((unsigned int *)&tab[h], c);
+            return -1;
         }
-    d = red.sum(dp);
-    W = red.max(wp);
-    int kp = 0, mn = INT_MAX, mx = -1;
-    for (int s = gtid; s < cap; s += gsize)
-        if (key[s] != kEmpty && (int)cnt[s] == W) {
-            kp++;
-            mn = min(mn, (int)key[s]);
-            mx = max(mx, (int)key[s]);
+        if ((uint32_t)(cur >> kT64GenShift) != gen) {  // stale: claim it
+            const unsigned long long prev = atomicCAS(&tab[h], cur, tag | c);
+            if (prev == cur) return (int)h;
+            cur = prev;  // taken meanwhile: look at it again
+            continue;
         }
-    k = red.sum(kp);
-    cmin = red.min(mn);
-    cmax = red.max(mx);
-    rmin = rmax = 0;
-    if (k > 1) {
-        int a0 = 0, a1 = 0;
-        for (int s = gtid; s < cap; s += gsize)
-            if (key[s] != kEmpty) {
-                a0 += (int)key[s] < cmin;
-                a1 += (int)key[s] < cmax;
-            }
-        rmin = red.sum(a0);
-        rmax = red.sum(a1);
+        h = (h + 1 == cap) ? 0 : h + 1;
+        cur = *(volatile unsigned long long *)&tab[h];
     }
 }
 
-struct WarpRed {
-    __device__ int sum(int x) const { return __reduce_add_sync(kFull, x); }
-    __device__ int max(int x) const { return __reduce_max_sync(kFull, x); }
-    __device__ int min(int x) const { return __reduce_min_sync(kFull, x); }
+// Per-vertex summary: distinct labels d, maximum count W, number k of labels with count
+// W and the smallest / largest of them.
+struct Sum5 {
+    int d, W, k, mn, mx;
 };
 
-template <int THREADS>
-struct BlockRedT {
-    int *buf;  // THREADS / 32 ints
-    __device__ int combine(int x, int op) const
-    {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        int w = op == 0 ? __reduce_add_sync(kFull, x) : op == 1 ? __reduce_max_sync(kFull, x) : __reduce_min_sync(kFull, x);
-        __syncthreads();
-        if (lane == 0) buf[warp] = w;
-        __syncthreads();
-        int r = buf[0];
-        for (int i = 1; i < THREADS / 32; ++i) r = op == 0 ? r + buf[i] : op == 1 ? ::max(r, buf[i]) : ::min(r, buf[i]);
-        return r;
-    }
-    __device__ int sum(int x) const { return combine(x, 0); }
-    __device__ int max(int x) const { return combine(x, 1); }
-    __device__ int min(int x) const { return combine(x, 2); }
-};
+__device__ __forceinline__ Sum5 sum5_empty() { return Sum5{0, 0, 0, INT_MAX, -1}; }
 
-// Write the occupied (label, count) entries of a tied vertex's region to its spill
-// positions (unsorted), by one warp.
-__device__ void spill_region_warp(const uint32_t *key, const uint32_t *cnt, int cap, int32_t *rl, uint16_t *rc,
-                                  int lane)
+__device__ __forceinline__ void sum5_add(Sum5 &s, int lab, int c)
 {
-    int base = 0;
-    for (int s0 = 0; s0 < cap; s0 += 32) {
-        const int s = s0 + lane;
-        const bool occ = s < cap && key[s] != kEmpty;
+    s.d++;
+    if (c > s.W) {
+        s.W = c;
+        s.k = 1;
+        s.mn = s.mx = lab;
+    } else if (c == s.W) {
+        s.k++;
+        s.mn = min(s.mn, lab);
+        s.mx = max(s.mx, lab);
+    }
+}
+
+__device__ __forceinline__ Sum5 sum5_warp(const Sum5 &s)
+{
+    Sum5 r;
+    r.W = __reduce_max_sync(kFull, s.W);
+    const bool top = s.W == r.W;
+    r.d = __reduce_add_sync(kFull, s.d);
+    r.k = __reduce_add_sync(kFull, top ? s.k : 0);
+    r.mn = __reduce_min_sync(kFull, top ? s.mn : INT_MAX);
+    r.mx = __reduce_max_sync(kFull, top ? s.mx : -1);
+    return r;
+}
+
+// Scan slots [t0, cap) step `stride` of the current generation into a partial summary.
+__device__ __forceinline__ Sum5 t64_scan(const unsigned long long *tab, int cap, int t0, int stride, uint32_t gen)
+{
+    Sum5 s = sum5_empty();
+    for (int i = t0; i < cap; i += stride) {
+        const unsigned long long x = tab[i];
+        if ((uint32_t)(x >> kT64GenShift) == gen) sum5_add(s, (int)((x >> 14) & 0x7FFFFFFF), (int)(x & kT64CntMask));
+    }
+    return s;
+}
+
+// Ranks of cmin and cmax among the vertex's distinct labels (partial counts).
+__device__ __forceinline__ void t64_ranks(const unsigned long long *tab, int cap, int t0, int stride, uint32_t gen,
+                                          int cmin, int cmax, int &a0, int &a1)
+{
+    a0 = a1 = 0;
+    for (int i = t0; i < cap; i += stride) {
+        const unsigned long long x = tab[i];
+        if ((uint32_t)(x >> kT64GenShift) == gen) {
+            const int lab = (int)((x >> 14) & 0x7FFFFFFF);
+            a0 += lab < cmin;
+            a1 += lab < cmax;
+        }
+    }
+}
+
+// Write the vertex's (label, count) entries, unsorted, to its spill positions; `ctr` is
+// a shared counter the group has zeroed.
+__device__ __forceinline__ void t64_spill(const unsigned long long *tab, int cap, int t0, int stride, uint32_t gen,
+                                          int32_t *rl, uint16_t *rc, int *ctr)
+{
+    const int lane = threadIdx.x & 31;
+    for (int i0 = t0 - lane; i0 < cap; i0 += stride) {  // warp-uniform trip count
+        const int i = i0 + lane;
+        const unsigned long long x = i < cap ? tab[i] : 0ull;
+        const bool occ = i < cap && (uint32_t)(x >> kT64GenShift) == gen;
         const unsigned m = __ballot_sync(kFull, occ);
+        if (!m) continue;
+        int base = 0;
+        if (lane == __ffs(m) - 1) base = atomicAdd(ctr, __popc(m));
+        base = __shfl_sync(kFull, base, __ffs(m) - 1);
         if (occ) {
             const int at = base + __popc(m & ((1u << lane) - 1));
-            rl[at] = (int32_t)key[s];
-            rc[at] = (uint16_t)cnt[s];
+            rl[at] = (int32_t)((x >> 14) & 0x7FFFFFFF);
+            rc[at] = (uint16_t)(x & kT64CntMask);
         }
-        base += __popc(m);
     }
 }
 
+// Insert one row of gathered labels: lanes holding the same label add once when
+// `aggregate` (heavy labels would otherwise serialise on one slot).
+__device__ __forceinline__ void t64_insert_row(unsigned long long *tab, uint32_t cap, uint32_t gen, uint32_t lb,
+                                               bool aggregate)
+{
+    if (aggregate) {
+        const unsigned same = __match_any_sync(kFull, lb);
+        const int lane = threadIdx.x & 31;
+        if (lb != kEmpty && lane == __ffs(same) - 1) t64_insert(tab, cap, gen, lb, (uint32_t)__popc(same));
+    } else if (lb != kEmpty) {
+        t64_insert(tab, cap, gen, lb, 1u);
+    }
+}
+
+// Aggregate inserts when the vertex had at most half as many distinct labels as
+// neighbours in the previous iteration (agg_mode 0); always (1); never (2).
+__device__ __forceinline__ bool use_aggregation(const PipeArgs &p, int v, int deg)
+{
+    const int mode = p.disp->agg_mode;
+    return mode == 1 || (mode == 0 && 2 * p.dcnt[v] <= deg);
+}
+
+// Finish a counted vertex: per-vertex state, label or tied list.  One thread.
+__device__ __forceinline__ void finish_counted(const PipeArgs &p, int v, const Sum5 &s, int rmin, int rmax,
+                                               unsigned long long &changes)
+{
+    p.dcnt[v] = s.d;
+    p.sm_kw[v] = s.k | (s.W << 16);
+    const int32_t old = __ldg(&p.lab_in[v]);
+    if (s.k == 1) {
+        p.lab_out[v] = s.mn;
+        count_change(changes, s.mn, old);
+        note_change(p, v, s.mn, old);
+    } else {
+        p.sm_c0[v] = s.mn;
+        p.sm_c1[v] = s.mx;
+        p.sm_r[v] = rmin | (rmax << 16);
+        p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+    }
+}
+
+// Frontier: a clean vertex keeps its counts; it is re-resolved if tied, else keeps its
+// label.  One thread.
+__device__ __forceinline__ void carry_clean(const PipeArgs &p, int v)
+{
+    if ((p.sm_kw[v] & 0xFFFF) > 1) p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+    else p.lab_out[v] = __ldg(&p.lab_in[v]);
+}
+
+// One warp per mid vertex (33..256 neighbours): a 512-slot table of 32-bit keys and
+// counts per warp, cleared per vertex (at warp scope plain 32-bit atomics beat the
+// generation-tagged slots).
 __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
 {
     __shared__ uint32_t skey[kMidWarps][kMidSCap];
     __shared__ uint32_t scnt[kMidWarps][kMidSCap];
     if (!ctl_active(p.ctl)) return;
+    const bool fr = frontier_on(p);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = blockIdx.x * kMidWarps + w;
     const int nw = gridDim.x * kMidWarps;
     unsigned long long changes = 0;
     uint32_t *key = skey[w], *cnt = scnt[w];
-    for (int i = gw; i < p.nmid_s; i += nw) {
+    const int nwarp_v = p.disp->pos1;  // the degree-sorted mid list's prefix of warp vertices
+    for (int i = gw; i < nwarp_v; i += nw) {
         const int v = p.mid_v[i];
-        if (p.dirty && !p.dirty[v]) {
-            if (lane == 0) {
-                if ((p.sm_kw[v] & 0xFFFF) > 1) p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
-                else p.lab_out[v] = __ldg(&p.lab_in[v]);
-            }
+        if (fr && !p.dirty[v]) {
+            if (lane == 0) carry_clean(p, v);
             continue;
         }
         const int64_t o0 = __ldg(&p.off[v]);
@@ -368,6 +472,7 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
         for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[u]]) : kEmpty;
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
+            if (u * 32 >= deg) break;  // warp-uniform
             // lanes holding the same label add once (heavy labels would serialise)
             const unsigned same = __match_any_sync(kFull, lb[u]);
             if (lb[u] == kEmpty || lane != __ffs(same) - 1) continue;
@@ -382,58 +487,130 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
             }
         }
         __syncwarp();
-        int d, W, k, cmin, cmax, rmin, rmax;
-        table_summary(key, cnt, cap, lane, 32, WarpRed{}, d, W, k, cmin, cmax, rmin, rmax);
-        const bool tied = k > 1;
-        if (tied) spill_region_warp(key, cnt, cap, p.run_lab + (o0 - p.nbr_shift), p.run_cnt + (o0 - p.nbr_shift), lane);
-        if (lane == 0) {
-            p.dcnt[v] = d;
-            p.sm_kw[v] = k | (W << 16);
-            const int32_t old = __ldg(&p.lab_in[v]);
-            if (!tied) {
-                p.lab_out[v] = cmin;
-                count_change(changes, cmin, old);
-                note_change(p, v, cmin, old);
-            } else {
-                p.sm_c0[v] = cmin;
-                p.sm_c1[v] = cmax;
-                p.sm_r[v] = rmin | (rmax << 16);
-                p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+        Sum5 part = sum5_empty();
+        for (int s = lane; s < cap; s += 32)
+            if (key[s] != kEmpty) sum5_add(part, (int)key[s], (int)cnt[s]);
+        const Sum5 sm = sum5_warp(part);
+        int rmin = 0, rmax = 0;
+        if (sm.k > 1) {
+            int a0 = 0, a1 = 0;
+            for (int s = lane; s < cap; s += 32)
+                if (key[s] != kEmpty) {
+                    a0 += (int)key[s] < sm.mn;
+                    a1 += (int)key[s] < sm.mx;
+                }
+            rmin = __reduce_add_sync(kFull, a0);
+            rmax = __reduce_add_sync(kFull, a1);
+            if (sm.k > 2) {  // resolving may need the runs themselves (unsorted)
+                int32_t *rl = p.run_lab + (o0 - p.nbr_shift);
+                uint16_t *rc = p.run_cnt + (o0 - p.nbr_shift);
+                int base = 0;
+                for (int s0 = 0; s0 < cap; s0 += 32) {
+                    const int s = s0 + lane;
+                    const bool occ = key[s] != kEmpty;  // cap is a multiple of 64
+                    const unsigned m = __ballot_sync(kFull, occ);
+                    if (occ) {
+                        const int at = base + __popc(m & ((1u << lane) - 1));
+                        rl[at] = (int32_t)key[s];
+                        rc[at] = (uint16_t)cnt[s];
+                    }
+                    base += __popc(m);
+                }
             }
         }
+        if (lane == 0) finish_counted(p, v, sm, rmin, rmax, changes);
         __syncwarp();
     }
     flush_changes(changes, p.ctl);
 }
 
-// One CTA of THREADS threads per vertex of degree <= SLOTS/2 (label slots in dynamic
-// shared memory: keys then counts), for the vertices mid_v[first .. first + count).
+// Block-wide Sum5 / pair reductions through shared memory (two barriers each).
+template <int THREADS>
+struct BlockRed5 {
+    int (*buf)[32];  // [5][32]
+    __device__ Sum5 reduce(Sum5 s) const
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        s = sum5_warp(s);
+        if (lane == 0) {
+            buf[0][warp] = s.d;
+            buf[1][warp] = s.W;
+            buf[2][warp] = s.k;
+            buf[3][warp] = s.mn;
+            buf[4][warp] = s.mx;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            Sum5 t = sum5_empty();
+            if (lane < THREADS / 32) t = Sum5{buf[0][lane], buf[1][lane], buf[2][lane], buf[3][lane], buf[4][lane]};
+            t = sum5_warp(t);
+            if (lane == 0) {
+                buf[0][0] = t.d;
+                buf[1][0] = t.W;
+                buf[2][0] = t.k;
+                buf[3][0] = t.mn;
+                buf[4][0] = t.mx;
+            }
+        }
+        __syncthreads();
+        const Sum5 r{buf[0][0], buf[1][0], buf[2][0], buf[3][0], buf[4][0]};
+        return r;
+    }
+    __device__ void reduce2(int &a, int &b) const
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        a = __reduce_add_sync(kFull, a);
+        b = __reduce_add_sync(kFull, b);
+        __syncthreads();  // buf may still be read from the previous reduction
+        if (lane == 0) {
+            buf[0][warp] = a;
+            buf[1][warp] = b;
+        }
+        __syncthreads();
+        int x = 0, y = 0;
+        for (int i = 0; i < THREADS / 32; ++i) {
+            x += buf[0][i];
+            y += buf[1][i];
+        }
+        a = x;
+        b = y;
+    }
+};
+
+// One CTA of THREADS threads per vertex of degree <= SLOTS/2 (table of SLOTS 64-bit
+// slots in dynamic shared memory), for a range of the degree-sorted mid list.
 template <int THREADS, int SLOTS>
-__global__ void __launch_bounds__(THREADS) count_cta_kernel(PipeArgs p, int first, int count)
+__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 6) count_cta_kernel(PipeArgs p, int which)
 {
-    extern __shared__ __align__(16) uint32_t cta_smem[];
-    uint32_t *key = cta_smem, *cnt = cta_smem + SLOTS;
-    __shared__ int red[THREADS / 32];
+    extern __shared__ __align__(16) unsigned long long cta_tab[];
+    __shared__ int red[5][32];
+    __shared__ int sctr;
     if (!ctl_active(p.ctl)) return;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // which 0: mid list [pos1, pos2); which 1: [pos2, end)
+    const int first = which == 0 ? p.disp->pos1 : p.disp->pos2;
+    const int count = (which == 0 ? p.disp->pos2 : p.nmid_s + p.nmid_l + p.nmid_x) - first;
+    const bool fr = frontier_on(p);
+    const int tid = threadIdx.x;
+    const BlockRed5<THREADS> br{red};
     unsigned long long changes = 0;
+    for (int s = tid; s < SLOTS; s += THREADS) cta_tab[s] = 0ull;
+    uint32_t gen = 0;
+    __syncthreads();
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         const int v = p.mid_v[first + i];
-        if (p.dirty && !p.dirty[v]) {
-            if (tid == 0) {
-                if ((p.sm_kw[v] & 0xFFFF) > 1) p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
-                else p.lab_out[v] = __ldg(&p.lab_in[v]);
-            }
+        if (fr && !p.dirty[v]) {
+            if (tid == 0) carry_clean(p, v);
             continue;
+        }
+        if (++gen > kT64GenMax) {
+            for (int s = tid; s < SLOTS; s += THREADS) cta_tab[s] = 0ull;
+            __syncthreads();
+            gen = 1;
         }
         const int64_t o0 = __ldg(&p.off[v]);
         const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
-        const int cap = 2 * pad32(deg);
-        for (int s = tid; s < cap; s += THREADS) {
-            key[s] = kEmpty;
-            cnt[s] = 0;
-        }
-        __syncthreads();
+        const uint32_t cap = 2 * pad32(deg);
+        const bool agg = use_aggregation(p, v, deg);
         // gather in rounds of PER loads per thread in flight together
         constexpr int PER = 8;
         for (int base = 0; base < deg; base += THREADS * PER) {
@@ -448,47 +625,29 @@ __global__ void __launch_bounds__(THREADS) count_cta_kernel(PipeArgs p, int firs
             for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[u]]) : kEmpty;
 #pragma unroll
             for (int u = 0; u < PER; ++u) {
-                // lanes holding the same label add once (heavy labels would serialise)
-                const unsigned same = __match_any_sync(kFull, lb[u]);
-                if (lb[u] == kEmpty || lane != __ffs(same) - 1) continue;
-                uint32_t h = hslot(lb[u], (uint32_t)cap);
-                for (;;) {
-                    const uint32_t prev = atomicCAS(&key[h], kEmpty, lb[u]);
-                    if (prev == kEmpty || prev == lb[u]) {
-                        atomicAdd(&cnt[h], (uint32_t)__popc(same));
-                        break;
-                    }
-                    h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
-                }
+                if (base + u * THREADS >= deg) break;  // block-uniform
+                t64_insert_row(cta_tab, cap, gen, lb[u], agg);
             }
         }
         __syncthreads();
-        int d, W, k, cmin, cmax, rmin, rmax;
-        table_summary(key, cnt, cap, tid, THREADS, BlockRedT<THREADS>{red}, d, W, k, cmin, cmax, rmin, rmax);
-        const bool tied = k > 1;
-        if (tied && warp == 0)
-            spill_region_warp(key, cnt, cap, p.run_lab + (o0 - p.nbr_shift), p.run_cnt + (o0 - p.nbr_shift), lane);
-        if (tid == 0) {
-            p.dcnt[v] = d;
-            p.sm_kw[v] = k | (W << 16);
-            const int32_t old = __ldg(&p.lab_in[v]);
-            if (!tied) {
-                p.lab_out[v] = cmin;
-                count_change(changes, cmin, old);
-                note_change(p, v, cmin, old);
-            } else {
-                p.sm_c0[v] = cmin;
-                p.sm_c1[v] = cmax;
-                p.sm_r[v] = rmin | (rmax << 16);
-                p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+        const Sum5 s = br.reduce(t64_scan(cta_tab, (int)cap, tid, THREADS, gen));
+        int rmin = 0, rmax = 0;
+        if (s.k > 1) {
+            t64_ranks(cta_tab, (int)cap, tid, THREADS, gen, s.mn, s.mx, rmin, rmax);
+            br.reduce2(rmin, rmax);
+            if (s.k > 2) {
+                if (tid == 0) sctr = 0;
+                __syncthreads();
+                t64_spill(cta_tab, (int)cap, tid, THREADS, gen, p.run_lab + (o0 - p.nbr_shift),
+                          p.run_cnt + (o0 - p.nbr_shift), &sctr);
             }
         }
+        if (tid == 0) finish_counted(p, v, s, rmin, rmax, changes);
         __syncthreads();
     }
     flush_changes(changes, p.ctl);
 }
 
-// big vertices: distinct counts into dcnt before the scan
 __global__ void big_dcnt_kernel(IterArgs a, int32_t *dcnt)
 {
     if (!ctl_active(a.ctl)) return;
@@ -795,13 +954,18 @@ __global__ void __launch_bounds__(kTB) resolve_mid_kernel(PipeArgs p)
 
 // Frontier: mark the neighbours of every vertex that changed in the previous iteration
 // (the graph is symmetric, so they are exactly the vertices whose neighbour labels
-// changed).  One warp per changed vertex.
+// changed).  One warp per changed vertex.  When the dispatcher chose a full recount for
+// this iteration (e.g. most labels changed, so marking would touch most of the graph)
+// nothing is marked and ctl->frontier_off tells the count kernels.
 __global__ void __launch_bounds__(kTB) mark_dirty_kernel(const int64_t *off, const int32_t *nbr,
-                                                         const int32_t *changed, int nchanged_cap, Ctl *ctl,
+                                                         const int32_t *changed, const DispatchState *disp, Ctl *ctl,
                                                          uint8_t *dirty)
 {
     const int lane = threadIdx.x & 31;
-    const int nc = min(*((volatile int *)&ctl->changed_n), nchanged_cap);
+    const int nc = *((volatile int *)&ctl->changed_n);
+    const bool dense = !disp->frontier;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->frontier_off = dense ? 1 : 0;
+    if (dense) return;
     for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nc; i += (gridDim.x * blockDim.x) >> 5) {
         const int u = changed[i];
         const int64_t e0 = off[u], e1 = off[u + 1];
@@ -830,6 +994,7 @@ struct AllCandidates {
 __global__ void __launch_bounds__(kTB) first_iteration_kernel(PipeArgs p, int64_t n, int64_t m)
 {
     if (!ctl_active(p.ctl)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) p.ctl->N = m;  // one run per CSR entry
     unsigned long long changes = 0;
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
         const int64_t o0 = __ldg(&p.off[v]);
@@ -842,22 +1007,75 @@ __global__ void __launch_bounds__(kTB) first_iteration_kernel(PipeArgs p, int64_
             nl = __ldg(&p.nbr[o0 + r]);
         }
         p.lab_out[v] = nl;
+        p.dcnt[v] = (int32_t)deg;  // every neighbour label distinct (insert-aggregation hint)
         count_change(changes, nl, old);
         note_change(p, (int32_t)v, nl, old);
     }
     flush_changes(changes, p.ctl);
 }
 
-// Sets *bad when some adjacency list is not strictly increasing.
-__global__ void adjacency_order_kernel(const int64_t *off, const int32_t *nbr, int64_t n, int *bad)
+// One pass over the resident CSR at setup (warp per 32 consecutive vertices, lanes over
+// the warp's edge range, row of each edge by a shuffle binary search over the 33 offsets):
+//   out[0] += adjacent entries of one row that are not strictly increasing
+//             (0 enables the first-iteration shortcut);
+//   out[1], out[2] += sum over entries (v, u) of g(v)k(u) - g(u)k(v) (mod 2^64) for two
+//             hash pairs g, k.  The form is antisymmetric, so every graph whose edge
+//             multiset is symmetric sums to 0 in both; an asymmetric one does so only by a
+//             hash collision (about 2^-64 per sum).  Both 0 enables the frontier, whose
+//             dirty marking pushes along out-edges.
+__device__ __forceinline__ uint64_t adj_hash(uint64_t x, uint64_t salt)
 {
-    int b = 0;
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t e1 = off[v + 1];
-        for (int64_t e = off[v] + 1; e < e1 && !b; ++e)
-            if (nbr[e] <= nbr[e - 1]) b = 1;
+    return splitmix64_mix(x * 0x9E3779B97F4A7C15ull + salt);
+}
+
+__global__ void __launch_bounds__(kTB) adjacency_check_kernel(const int64_t *off, const int32_t *nbr, int64_t n,
+                                                              unsigned long long *out)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nwb = (n + 31) >> 5;
+    unsigned long long desc = 0, s1 = 0, s2 = 0;
+    for (int64_t wb = (int64_t)(blockIdx.x * blockDim.x + threadIdx.x) >> 5; wb < nwb;
+         wb += (int64_t)(gridDim.x * blockDim.x) >> 5) {
+        const int64_t vb = wb << 5;
+        const int64_t o = off[min(vb + lane, n)];  // lanes past n hold off[n]
+        const int64_t oend = off[min(vb + 32, n)];
+        const int64_t e_begin = __shfl_sync(kFull, o, 0);
+        int32_t carry = 0;  // last entry of the previous chunk
+        for (int64_t c = e_begin; c < oend; c += 32) {
+            const int64_t e = c + lane;
+            int r = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int64_t oc = __shfl_sync(kFull, o, r + step);
+                if (oc <= e) r += step;
+            }
+            const bool valid = e < oend;
+            const int32_t u = valid ? __ldg(&nbr[e]) : 0;
+            int32_t prev = __shfl_up_sync(kFull, u, 1);
+            if (lane == 0) prev = carry;
+            carry = __shfl_sync(kFull, u, 31);
+            const int64_t row_start = __shfl_sync(kFull, o, r);
+            if (valid) {
+                if (e != row_start && u <= prev) ++desc;
+                const uint64_t v = (uint64_t)(vb + r);
+                s1 += adj_hash(v, 0x1234567ull) * adj_hash((uint64_t)u, 0xABCDEF1ull) -
+                      adj_hash((uint64_t)u, 0x1234567ull) * adj_hash(v, 0xABCDEF1ull);
+                s2 += adj_hash(v, 0x7777777ull) * adj_hash((uint64_t)u, 0x3141592ull) -
+                      adj_hash((uint64_t)u, 0x7777777ull) * adj_hash(v, 0x3141592ull);
+            }
+        }
     }
-    if (__any_sync(kFull, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+#pragma unroll
+    for (int sh = 16; sh > 0; sh >>= 1) {
+        desc += __shfl_xor_sync(kFull, desc, sh);
+        s1 += __shfl_xor_sync(kFull, s1, sh);
+        s2 += __shfl_xor_sync(kFull, s2, sh);
+    }
+    if (lane == 0) {
+        if (desc) atomicAdd(&out[0], desc);
+        atomicAdd(&out[1], s1);
+        atomicAdd(&out[2], s2);
+    }
 }
 
 }  // namespace galp

@@ -17,15 +17,20 @@ extern "C" {
 
 typedef struct {
     int64_t n, m;          /* vertices, CSR entries */
-    int64_t m_big;         /* CSR entries of vertices above 2048 neighbours (global-table path) */
+    int64_t m_big;         /* CSR entries of vertices above 12288 neighbours (global-table path) */
     int64_t npacks;        /* packs of vertices with <= 32 neighbours (one warp each) */
     int64_t nmid;          /* vertices with 33..256 neighbours (one warp each) */
-    int64_t nlarge;        /* vertices with 257..2048 neighbours (one CTA each) */
+    int64_t nlarge;        /* vertices with 257..12288 neighbours (one CTA each, on-chip table) */
     int64_t nbig;          /* vertices on the global-table path */
     int64_t table_slots;   /* global hash-table slots of those vertices (largest scope) */
-    int32_t launches_per_iter; /* kernels launched per iteration (upper bound) */
-    int32_t pad;
+    int32_t launches_per_iter; /* kernels launched per dense iteration (upper bound) */
+    int32_t flags;         /* GALP_SCHED_* bits */
+    int64_t launches;      /* kernels launched by the context's runs so far (setup excluded) */
 } galp_sched_info;
+
+#define GALP_SCHED_SORTED 1     /* every adjacency list strictly increasing */
+#define GALP_SCHED_SYMMETRIC 2  /* edge multiset symmetric (checked by an edge checksum) */
+#define GALP_SCHED_FRONTIER 4   /* frontier requested and usable (policy 0, symmetric graph) */
 
 typedef struct {
     double pipe_ms;        /* count + scan + resolve kernels: summed device time */
@@ -37,11 +42,75 @@ typedef struct {
     int32_t pad;
 } galp_kernel_times;
 
+typedef struct {
+    char name[48];         /* kernel (or "memset") */
+    double ms;             /* device time between the events around it, summed */
+    int64_t launches;
+} galp_kernel_stat;
+
+/* Kernel variant knobs.  Every variant computes the same labels; they differ in speed. */
+typedef struct {
+    int32_t agg_mode;      /* warp-aggregated table inserts: 0 auto (by last distinct count), 1 always,
+                              2 never (default) */
+    float frontier_frac;   /* fixed rule, frontier mode: an iteration after more than this fraction
+                              of labels changed recounts every vertex (default 0.05) */
+    float learned_margin;  /* learned rule: predicted log gain needed to leave the fixed rule's
+                              choice (default 0.03) */
+    int32_t pad[5];
+} galp_variant;
+
+/* One row of the in-core variant table (every row computes the same labels). */
+typedef struct {
+    int32_t agg_mode;          /* CTA-table inserts: 1 warp-aggregated, 2 plain */
+    int32_t frontier;          /* 1 = skip vertices whose neighbour labels did not change */
+    int32_t warp_max_degree;   /* mid vertices up to this degree: one warp each */
+    int32_t cta256_max_degree; /* then 256-thread CTAs up to this degree, 1024-thread CTAs above */
+    int32_t pos1, pos2;        /* the same split as positions in the degree-sorted mid list */
+} galp_dispatch_row;
+
+#define GALP_DISPATCH_FEATURES 24
+#define GALP_DISPATCH_HIDDEN 64
+#define GALP_DISPATCH_VARIANTS 16
+
 int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info);
+
+/* Per-iteration dispatch: mode 0 = fixed rule (default), 1 = learned MLP (weights: the
+ * galp_mlp_size(24, 64, 16) parameters of a galp_mlp, or NULL to keep those loaded; the
+ * library's trained weights are loaded by opts.dispatch = 1), 2 = forced_variant every
+ * iteration. */
+int galp_dispatch_set(galp_ctx *ctx, int32_t mode, int32_t forced_variant, const float *weights, int64_t count);
+/* Features (count x 24) and chosen variant (-1 = first-iteration shortcut) of the last
+ * run's iterations. */
+int galp_dispatch_log(galp_ctx *ctx, float *features, int32_t *variants, int32_t cap_iters, int32_t *count);
+int galp_dispatch_table(galp_ctx *ctx, galp_dispatch_row *rows, int32_t cap, int32_t *count);
+/* Device time of every in-core iteration since the last call (profile level >= 1). */
+int galp_profile_iterations(galp_ctx *ctx, float *ms, int32_t cap, int32_t *count);
+
+/* The dispatcher's network as a trainable object: nin -> nhid -> nhid -> nout, ReLU,
+ * masked mean squared error, AdamW; forward, gradient and training run on the GPU. */
+typedef struct galp_mlp galp_mlp;
+int64_t galp_mlp_size(int32_t nin, int32_t nhid, int32_t nout);
+int galp_mlp_create(int32_t nin, int32_t nhid, int32_t nout, uint64_t seed, galp_mlp **out);
+int galp_mlp_set_weights(galp_mlp *mlp, const float *w, int64_t count);
+int galp_mlp_get_weights(galp_mlp *mlp, float *w, int64_t count);
+int galp_mlp_forward(galp_mlp *mlp, const float *x, int32_t batch, float *y);
+/* loss and its gradient (parameter layout) on one batch; mask may be NULL (all ones) */
+int galp_mlp_loss_grad(galp_mlp *mlp, const float *x, const float *target, const float *mask, int32_t batch,
+                       float *loss, float *grad);
+/* `steps` full-batch AdamW steps; loss_curve[steps] may be NULL */
+int galp_mlp_train(galp_mlp *mlp, const float *x, const float *target, const float *mask, int32_t batch,
+                   int32_t steps, float lr, float weight_decay, float *loss_curve);
+void galp_mlp_destroy(galp_mlp *mlp);
+int galp_set_variant(galp_ctx *ctx, const galp_variant *v);
+int galp_get_variant(galp_ctx *ctx, galp_variant *v);
 /* Record CUDA events around each kernel group of every following iteration. */
-int galp_profile(galp_ctx *ctx, int32_t enable);
+/* 0 = off, 1 = events around kernel groups, 2 = also around every kernel */
+int galp_profile(galp_ctx *ctx, int32_t level);
 /* Wait for the stream, sum and clear the recorded kernel times. */
 int galp_profile_read(galp_ctx *ctx, galp_kernel_times *out);
+/* Per-kernel totals since the last call (level 2), in order of first launch; writes up to
+ * cap entries and the number of distinct kernels to *count. */
+int galp_profile_kernels(galp_ctx *ctx, galp_kernel_stat *out, int32_t cap, int32_t *count);
 
 /* Write nedges raw R-MAT edge keys (u << 32 | v) into device memory d_out, on
  * `stream` (cudaStream_t as void*), with the same sampler as galp_gen_rmat. */
