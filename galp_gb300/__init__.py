@@ -99,6 +99,15 @@ def load_library() -> ctypes.CDLL:
     L.galp_debug_resolve_rank.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int32, P,
                                           ctypes.c_int32]
     L.galp_debug_resolve_rank.restype = ctypes.c_int32
+    L.galp_batch_create.argtypes = [P, P, ctypes.c_int64, ctypes.c_int64, P, ctypes.c_int32, ctypes.POINTER(Opts),
+                                    ctypes.POINTER(P)]
+    L.galp_batch_create.restype = ctypes.c_int
+    L.galp_batch_stats.argtypes = [P, ctypes.c_int32, ctypes.POINTER(Stats)]
+    L.galp_batch_stats.restype = ctypes.c_int
+    L.galp_batch_labels.argtypes = [P, ctypes.c_int32, P, ctypes.c_int64]
+    L.galp_batch_labels.restype = ctypes.c_int
+    L.galp_run_batch.argtypes = [P, ctypes.c_int32, ctypes.POINTER(Opts), ctypes.c_int32, P, P]
+    L.galp_run_batch.restype = ctypes.c_int
     _lib = L
     return L
 
@@ -233,6 +242,100 @@ class Propagator:
     @property
     def updates(self) -> list[int]:
         return list(self.stats.updates[: self.stats.iters_run])
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            load_library().galp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Batch:
+    """Many independent graphs clustered together (include/galp.h galp_batch_create): each
+    graph gets exactly the labels, iteration count and change counts of its own run.
+
+    Either `graphs` (a list of Graph, concatenated here) or one concatenated CSR:
+    `offsets` int64[n+1] and `neighbors` int32[m] with global IDs (numpy arrays, or
+    integer device pointers together with n and m) and `graph_v0` int64[count+1]."""
+
+    def __init__(self, graphs=None, *, offsets=None, neighbors=None, graph_v0=None, n=None, m=None, **opts):
+        L = load_library()
+        if graphs is not None:
+            sizes = np.array([g.n for g in graphs], np.int64)
+            graph_v0 = np.zeros(len(graphs) + 1, np.int64)
+            graph_v0[1:] = np.cumsum(sizes)
+            ecount = np.array([g.m for g in graphs], np.int64)
+            e0 = np.zeros(len(graphs) + 1, np.int64)
+            e0[1:] = np.cumsum(ecount)
+            offsets = np.concatenate([np.asarray(g.offsets[:-1], np.int64) + e0[i] for i, g in enumerate(graphs)]
+                                     + [np.array([e0[-1]], np.int64)])
+            neighbors = np.concatenate([np.asarray(g.neighbors, np.int64) + graph_v0[i]
+                                        for i, g in enumerate(graphs)]).astype(np.int32)
+        self.graph_v0 = np.ascontiguousarray(graph_v0, np.int64)
+        self.count = len(self.graph_v0) - 1
+        if isinstance(offsets, int):
+            off_p, nbr_p = offsets, neighbors
+            self.n, self.m = int(n), int(m)
+        else:
+            self._off = np.ascontiguousarray(offsets, np.int64)
+            self._nbr = np.ascontiguousarray(neighbors, np.int32)
+            off_p = self._off.ctypes.data
+            nbr_p = self._nbr.ctypes.data if len(self._nbr) else None
+            self.n, self.m = len(self._off) - 1, len(self._nbr)
+        self.opts = default_opts(**opts)
+        h = ctypes.c_void_p()
+        _check(L.galp_batch_create(off_p, nbr_p, self.n, self.m, self.graph_v0.ctypes.data, self.count,
+                                   ctypes.byref(self.opts), ctypes.byref(h)), "galp_batch_create")
+        self._h = h
+        self.stats = Stats()
+
+    def run(self, niter: int = 10):
+        _check(load_library().galp_run(self._h, niter, ctypes.byref(self.stats)), "galp_run")
+        return self.stats.f1, self.stats.f2
+
+    def enqueue(self, niter: int) -> None:
+        _check(load_library().galp_enqueue(self._h, niter), "galp_enqueue")
+
+    def sync(self) -> Stats:
+        _check(load_library().galp_sync(self._h, ctypes.byref(self.stats)), "galp_sync")
+        return self.stats
+
+    def set_stream(self, stream_ptr) -> None:
+        _check(load_library().galp_set_stream(self._h, stream_ptr), "galp_set_stream")
+
+    def labels(self, g: int) -> np.ndarray:
+        out = np.empty(int(self.graph_v0[g + 1] - self.graph_v0[g]), np.int32)
+        _check(load_library().galp_batch_labels(self._h, g, out.ctypes.data if len(out) else None, len(out)),
+               "galp_batch_labels")
+        return out
+
+    def all_labels(self) -> np.ndarray:
+        """Labels of every graph, concatenated in graph order (graph-local values)."""
+        out = np.empty(self.n, np.int32)
+        _check(load_library().galp_get_labels(self._h, out.ctypes.data if len(out) else None, len(out)),
+               "galp_get_labels")
+        return out
+
+    def graph_stats(self, g: int):
+        """(iterations run, change counts) of graph g in the last run."""
+        st = Stats()
+        _check(load_library().galp_batch_stats(self._h, g, ctypes.byref(st)), "galp_batch_stats")
+        return st.iters_run, [int(x) for x in st.updates[:st.iters_run]]
+
+    def tune(self, niter: int = 3) -> dict:
+        from . import tools
+        return tools.batch_tune(self, niter)
 
     def close(self) -> None:
         if getattr(self, "_h", None):

@@ -218,11 +218,12 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     build_schedule(sched, n, g.offsets, starts);
 
     GALP_CUDA(b_off.alloc(sizeof(int64_t) * (n + 1)));
-    GALP_CUDA(cudaMemcpyAsync(b_off.p, g.offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st));
+    GALP_CUDA(cudaMemcpyAsync(b_off.p, g.offsets, sizeof(int64_t) * (n + 1), cudaMemcpyDefault, st));
     h2d += sizeof(int64_t) * (n + 1);
     if (policy == 0) {
         GALP_CUDA(b_nbr[0].alloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
-        if (m) GALP_CUDA(cudaMemcpyAsync(b_nbr[0].p, g.neighbors, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
+        // host or device neighbours (batched callers may hand over a device array)
+        if (m) GALP_CUDA(cudaMemcpyAsync(b_nbr[0].p, g.neighbors, sizeof(int32_t) * m, cudaMemcpyDefault, st));
         h2d += sizeof(int32_t) * m;
     } else {
         const size_t cap = sizeof(int32_t) * std::max<int64_t>(sched.max_scope_edges, 1);
@@ -351,6 +352,55 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     return GALP_OK;
 }
 
+// Batched mode: `count` graphs concatenated into one CSR whose neighbour IDs are global;
+// graph g owns vertices [graph_v0[g], graph_v0[g+1]) and must not reach outside them.
+// Each graph keeps its own labels (local IDs), run positions, last vertex and early exit,
+// exactly as a separate in-core run of it.
+int Engine::setup_batch(const galp_csr &g, const int64_t *graph_v0, int32_t count, const galp_opts &o,
+                        cudaStream_t st, int64_t &h2d)
+{
+    if (o.policy != 0) return GALP_EUNSUPPORTED;
+    if (count < 1 || graph_v0[0] != 0 || graph_v0[count] != g.n) return GALP_EINVAL;
+    for (int32_t i = 0; i < count; ++i)
+        if (graph_v0[i + 1] < graph_v0[i]) return GALP_EINVAL;
+    batched = true;
+    G = count;
+    early_exit = o.early_exit ? 1 : 0;
+    galp_opts o2 = o;
+    o2.frontier = 0;
+    int rc = setup(g, o2, st, h2d);
+    if (rc) return rc;
+    if (!sched.big_v.empty()) return GALP_EUNSUPPORTED;  // global tables share one run-position scope
+    g_v0_h.assign(graph_v0, graph_v0 + count + 1);
+    g_last_h.assign(count, -1);
+    for (int32_t i = 0; i < count; ++i)
+        for (int64_t v = graph_v0[i + 1] - 1; v >= graph_v0[i]; --v)
+            if (g.offsets[v + 1] > g.offsets[v]) {
+                g_last_h[i] = (int32_t)v;
+                break;
+            }
+    batch_max_iter = GALP_MAX_ITERS;
+    int32_t *dummy = nullptr;
+    int64_t *dv0 = nullptr;
+    if ((rc = upload(b_g_v0, dv0, g_v0_h, st, h2d))) return rc;
+    if ((rc = upload(b_g_last, dummy, g_last_h, st, h2d))) return rc;
+    GALP_CUDA(b_g_base.alloc(sizeof(int64_t) * (count + 1)));
+    GALP_CUDA(b_g_active.alloc(sizeof(int32_t) * count));
+    GALP_CUDA(b_g_iters.alloc(sizeof(int32_t) * count));
+    GALP_CUDA(b_g_counts.alloc(sizeof(long long) * (size_t)count * batch_max_iter));
+    GALP_CUDA(cudaMemsetAsync(b_g_counts.p, 0, sizeof(long long) * (size_t)count * batch_max_iter, st));
+    GALP_CUDA(cudaMemsetAsync(b_g_iters.p, 0, sizeof(int32_t) * count, st));
+    // every edge stays inside its graph
+    GALP_CUDA(cudaMemsetAsync(b_bad.p, 0, sizeof(int), st));
+    batch_validate_kernel<<<(unsigned)std::min<int64_t>(count, 4096), kTB, 0, st>>>(
+        (const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p, dv0, count, (int *)b_bad.p);
+    GALP_CUDA(cudaGetLastError());
+    int bad = 0;
+    GALP_CUDA(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GALP_CUDA(cudaStreamSynchronize(st));
+    return bad ? GALP_EFORMAT : GALP_OK;
+}
+
 IterArgs Engine::big_args(const Scope &sc) const
 {
     IterArgs a{};
@@ -422,6 +472,12 @@ PipeArgs Engine::pipe_args(const Scope &sc) const
 {
     PipeArgs q{};
     q.disp = (const DispatchState *)b_disp.p + (&sc - sched.scopes.data());
+    if (batched) {
+        q.g_v0 = (const int64_t *)b_g_v0.p;
+        q.g_base = (const int64_t *)b_g_base.p;
+        q.g_last = (const int32_t *)b_g_last.p;
+        q.ngraphs = G;
+    }
     q.nbr_shift = (policy == 0) ? 0 : sc.e0;
     q.off = (const int64_t *)b_off.p;
     q.ctl = (Ctl *)b_ctl.p;
@@ -482,13 +538,13 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
     }
     if (prof.on) e0 = prof.mark(st);
     if (q.npacks) {
-        const int blocks = (int)std::min<int64_t>(((int64_t)q.npacks * 32 + 255) / 256, (int64_t)sms * 16);
+        const int blocks = (int)std::min<int64_t>(((int64_t)q.npacks * 32 + 255) / 256, (int64_t)sms * small_bps);
         count_small_kernel<<<blocks, 256, 0, st>>>(q);
         launched("count_small_kernel", st);
     }
     if (q.nmid_s + q.nmid_l + q.nmid_x) {
         // ranges of the degree-sorted mid list come from the dispatch state
-        count_mid_kernel<<<(int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1, (int64_t)sms * 6),
+        count_mid_kernel<<<(int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1, (int64_t)sms * mid_bps),
                            32 * kMidWarps, 0, st>>>(q);
         launched("count_mid_kernel", st);
         count_cta_kernel<kTB, 2 * kLargeMax>
@@ -512,7 +568,12 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         scan_apply_kernel<<<nblk, kTB, 0, st>>>(q);
         launched("scan_apply_kernel", st);
     }
-    resolve_small_kernel<<<sms * 4, kTB, 0, st>>>(q);
+    if (batched) {
+        batch_bases_kernel<<<(G + 1 + 255) / 256, 256, 0, st>>>((const int64_t *)b_g_v0.p, G, q.runbase, n,
+                                                                (const Ctl *)b_ctl.p, (int64_t *)b_g_base.p);
+        launched("batch_bases_kernel", st);
+    }
+    resolve_small_kernel<<<sms * resolve_bps, kTB, 0, st>>>(q);
     launched("resolve_small_kernel", st);
     if (q.nmid_s + q.nmid_l + q.nmid_x) {
         resolve_mid_kernel<<<sms * 2, kTB, 0, st>>>(q);
@@ -536,7 +597,14 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
 int Engine::enqueue_init(cudaStream_t st, int niter, long long thr)
 {
     prof.kstart(st);
-    if (n > 0) {
+    if (batched) {
+        batch_init_labels_kernel<<<(unsigned)std::min<int64_t>(G, (int64_t)sms * 8), kTB, 0, st>>>(
+            (const int64_t *)b_g_v0.p, G, (int32_t *)b_lab0.p);
+        launched("batch_init_labels_kernel", st);
+        batch_init_kernel<<<(G + 255) / 256, 256, 0, st>>>((int32_t *)b_g_active.p, (int32_t *)b_g_iters.p, G,
+                                                           niter > 0 ? 1 : 0);
+        launched("batch_init_kernel", st);
+    } else if (n > 0) {
         const unsigned blocks = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
         init_labels_kernel<<<blocks, 256, 0, st>>>((int32_t *)b_lab0.p, n);
         launched("init_labels_kernel", st);
@@ -621,8 +689,17 @@ int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
                 return rc;
             full_state = true;
         }
-        finalize_kernel<<<1, 1, 0, st>>>(ctl);
-        launched("finalize_kernel", st);
+        if (batched) {  // per-graph change counts, early exits and frozen graphs
+            batch_commit_kernel<<<(unsigned)std::min<int64_t>(G, (int64_t)sms * 8), kTB, 0, st>>>(
+                ctl, (const int64_t *)b_g_v0.p, G, lab[it & 1], lab[(it + 1) & 1], (int32_t *)b_g_active.p,
+                (int32_t *)b_g_iters.p, (long long *)b_g_counts.p, batch_max_iter, it, early_exit);
+            launched("batch_commit_kernel", st);
+            batch_finalize_kernel<<<1, 1024, 0, st>>>(ctl, (const int32_t *)b_g_active.p, G);
+            launched("batch_finalize_kernel", st);
+        } else {
+            finalize_kernel<<<1, 1, 0, st>>>(ctl);
+            launched("finalize_kernel", st);
+        }
         if (prof.on) prof.it_spans.push_back({it0, prof.mark(st)});
     }
     GALP_CUDA(cudaGetLastError());
@@ -738,7 +815,16 @@ const char *galp_strerror(int code)
     }
 }
 
+static int create_impl(const galp_csr *g, const galp_opts *o, galp_ctx **out, const int64_t *batch_v0,
+                       int32_t batch_count);
+
 int galp_create(const galp_csr *g, const galp_opts *o, galp_ctx **out)
+{
+    return create_impl(g, o, out, nullptr, 0);
+}
+
+static int create_impl(const galp_csr *g, const galp_opts *o, galp_ctx **out, const int64_t *batch_v0,
+                       int32_t batch_count)
 {
     if (!g || !out) return GALP_EINVAL;
     *out = nullptr;
@@ -762,7 +848,8 @@ int galp_create(const galp_csr *g, const galp_opts *o, galp_ctx **out)
     const double t0 = now_s();
     GALP_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
     ctx->stream = ctx->own_stream;
-    int rc = ctx->eng.setup(*g, opts, ctx->stream, ctx->h2d_setup);
+    int rc = batch_v0 ? ctx->eng.setup_batch(*g, batch_v0, batch_count, opts, ctx->stream, ctx->h2d_setup)
+                      : ctx->eng.setup(*g, opts, ctx->stream, ctx->h2d_setup);
     if (rc) return rc;
     if (opts.dispatch == 1) {  // the built-in trained dispatcher
 #if GALP_HAVE_TRAINED_DISPATCH
@@ -800,8 +887,33 @@ int galp_enqueue(galp_ctx *ctx, int32_t niter)
     if (!ctx || niter < 0) return GALP_EINVAL;
     GALP_CUDA(cudaSetDevice(ctx->opts.device));
     GALP_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    int rc = ctx->eng.policy == 0 ? ctx->eng.enqueue_run_incore(ctx->stream, niter, exit_threshold(ctx))
+    int rc;
+    if (ctx->eng.batched && !ctx->eng.prof.on) {
+        // the whole run (every iteration of every graph) as one CUDA-graph launch
+        if (ctx->graph_iters != niter) {
+            if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+            ctx->graph_exec = nullptr;
+            ctx->graph_iters = -1;
+            cudaGraph_t graph = nullptr;
+            GALP_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+            rc = ctx->eng.enqueue_run_incore(ctx->stream, niter, exit_threshold(ctx));
+            const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+            if (rc) {
+                if (graph) cudaGraphDestroy(graph);
+                return rc;
+            }
+            GALP_CUDA(ce);
+            const cudaError_t ie = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+            cudaGraphDestroy(graph);
+            GALP_CUDA(ie);
+            ctx->graph_iters = niter;
+        }
+        GALP_CUDA(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+        rc = GALP_OK;
+    } else {
+        rc = ctx->eng.policy == 0 ? ctx->eng.enqueue_run_incore(ctx->stream, niter, exit_threshold(ctx))
                                   : ctx->eng.run_outofcore(ctx->stream, niter, exit_threshold(ctx));
+    }
     if (rc) return rc;
     GALP_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->pending = true;
@@ -880,6 +992,7 @@ void galp_destroy(galp_ctx *ctx)
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -981,6 +1094,156 @@ int galp_profile_iterations(galp_ctx *ctx, float *ms, int32_t cap, int32_t *coun
     *count = (int32_t)P.it_ms.size();
     for (int32_t i = 0; i < cap && i < *count; ++i) ms[i] = P.it_ms[i];
     P.it_ms.clear();
+    return GALP_OK;
+}
+
+int galp_batch_create(const int64_t *offsets, const int32_t *neighbors, int64_t n, int64_t m,
+                      const int64_t *graph_v0, int32_t count, const galp_opts *opts, galp_ctx **out)
+{
+    if (!offsets || !graph_v0 || !out || n < 0 || m < 0 || count < 1) return GALP_EINVAL;
+    // the schedule is built on the host: bring device offsets over
+    std::vector<int64_t> host_off;
+    const int64_t *off = offsets;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, offsets) == cudaSuccess && pa.type == cudaMemoryTypeDevice) {
+        host_off.resize((size_t)n + 1);
+        GALP_CUDA(cudaMemcpy(host_off.data(), offsets, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost));
+        off = host_off.data();
+    } else {
+        (void)cudaGetLastError();
+    }
+    galp_csr g{neighbors, off, n, m};
+    return create_impl(&g, opts, out, graph_v0, count);
+}
+
+int galp_batch_stats(galp_ctx *ctx, int32_t graph, galp_stats *st)
+{
+    if (!ctx || !st || !ctx->eng.batched || graph < 0 || graph >= ctx->eng.G) return GALP_EINVAL;
+    galp::Engine &E = ctx->eng;
+    GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::memset(st, 0, sizeof(*st));
+    int32_t it = 0;
+    GALP_CUDA(cudaMemcpy(&it, (const int32_t *)E.b_g_iters.p + graph, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    st->iters_run = it;
+    std::vector<long long> c(E.batch_max_iter);
+    GALP_CUDA(cudaMemcpy(c.data(), (const long long *)E.b_g_counts.p + (size_t)graph * E.batch_max_iter,
+                         sizeof(long long) * E.batch_max_iter, cudaMemcpyDeviceToHost));
+    for (int i = 0; i < GALP_MAX_ITERS && i < it; ++i) st->updates[i] = (int64_t)c[i];
+    st->device_ms = ctx->device_ms;
+    return GALP_OK;
+}
+
+int galp_batch_labels(galp_ctx *ctx, int32_t graph, int32_t *labels, int64_t n)
+{
+    if (!ctx || !ctx->eng.batched || graph < 0 || graph >= ctx->eng.G) return GALP_EINVAL;
+    galp::Engine &E = ctx->eng;
+    const int64_t v0 = E.g_v0_h[graph], v1 = E.g_v0_h[graph + 1];
+    if (n != v1 - v0 || (n > 0 && !labels)) return GALP_EINVAL;
+    GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (n) GALP_CUDA(cudaMemcpy(labels, E.final_labels(ctx->iters) + v0, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    return GALP_OK;
+}
+
+int galp_run_batch(const galp_csr *graphs, int32_t count, const galp_opts *opts, int32_t niter, int32_t *labels_out,
+                   galp_stats *stats)
+{
+    if (!graphs || count < 1 || niter < 0) return GALP_EINVAL;
+    std::vector<int64_t> v0(count + 1, 0), off;
+    int64_t n = 0, m = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        const galp_csr &g = graphs[i];
+        if (g.n < 0 || g.m < 0 || !g.offsets || (g.m > 0 && !g.neighbors)) return GALP_EINVAL;
+        if (g.offsets[0] != 0 || g.offsets[g.n] != g.m) return GALP_EFORMAT;
+        n += g.n;
+        m += g.m;
+        v0[i + 1] = n;
+    }
+    if (n >= ((int64_t)1 << 31)) return GALP_EINVAL;
+    off.resize((size_t)n + 1);
+    std::vector<int32_t> nbr((size_t)std::max<int64_t>(m, 1));
+    int64_t e = 0;
+    for (int32_t i = 0; i < count; ++i) {
+        const galp_csr &g = graphs[i];
+        for (int64_t v = 0; v < g.n; ++v) off[v0[i] + v] = e + g.offsets[v];
+        for (int64_t k = 0; k < g.m; ++k) {
+            const int32_t u = g.neighbors[k];
+            if (u < 0 || u >= g.n) return GALP_EFORMAT;
+            nbr[e + k] = (int32_t)(u + v0[i]);
+        }
+        e += g.m;
+    }
+    off[n] = m;
+    galp_ctx *ctx = nullptr;
+    int rc = galp_batch_create(off.data(), nbr.data(), n, m, v0.data(), count, opts, &ctx);
+    if (rc) return rc;
+    rc = galp_run(ctx, niter, nullptr);
+    for (int32_t i = 0; !rc && i < count; ++i) {
+        if (labels_out) rc = galp_batch_labels(ctx, i, labels_out + v0[i], v0[i + 1] - v0[i]);
+        if (!rc && stats) rc = galp_batch_stats(ctx, i, &stats[i]);
+    }
+    galp_destroy(ctx);
+    return rc;
+}
+
+// Launch-shape autotuner for batched runs: coordinate descent over blocks per SM of the
+// small-vertex counting, mid-vertex counting and small-vertex resolve kernels, each
+// candidate timed on a probe run of niter iterations.
+int galp_batch_tune(galp_ctx *ctx, int32_t niter, galp_tune_result *res)
+{
+    if (!ctx || niter < 1) return GALP_EINVAL;
+    galp::Engine &E = ctx->eng;
+    int *knob[3] = {&E.small_bps, &E.mid_bps, &E.resolve_bps};
+    const int cand[3][4] = {{4, 8, 16, 32}, {2, 4, 6, 8}, {2, 4, 8, 16}};
+    float best_ms = 0.f;
+    int trials = 0;
+    auto probe = [&](float &ms) -> int {
+        int rc2 = galp_enqueue(ctx, niter);
+        if (rc2) return rc2;
+        GALP_CUDA(cudaEventSynchronize(ctx->ev1));
+        GALP_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        ++trials;
+        return GALP_OK;
+    };
+    const bool was_on = E.prof.on;
+    E.prof.on = true;  // enqueue directly while probing (no graph capture)
+    const int level = E.prof.level;
+    E.prof.level = 0;
+    int rc = probe(best_ms);  // warm-up
+    if (!rc) rc = probe(best_ms);
+    for (int k = 0; !rc && k < 3; ++k) {
+        int keep = *knob[k];
+        for (int c = 0; !rc && c < 4; ++c) {
+            if (cand[k][c] == keep) continue;
+            const int old = *knob[k];
+            *knob[k] = cand[k][c];
+            float ms = 0.f;
+            rc = probe(ms);
+            if (!rc && ms < best_ms) {
+                best_ms = ms;
+                keep = cand[k][c];
+            }
+            *knob[k] = old;
+        }
+        *knob[k] = keep;
+    }
+    E.prof.on = was_on;
+    E.prof.level = level;
+    E.prof.spans[0].clear();
+    E.prof.spans[1].clear();
+    E.prof.spans[2].clear();
+    E.prof.it_spans.clear();
+    E.prof.used = 0;
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);  // recapture with the chosen shapes
+    ctx->graph_exec = nullptr;
+    ctx->graph_iters = -1;
+    if (rc) return rc;
+    if (res) {
+        res->small_blocks_per_sm = E.small_bps;
+        res->mid_blocks_per_sm = E.mid_bps;
+        res->resolve_blocks_per_sm = E.resolve_bps;
+        res->trials = trials;
+        res->best_ms = best_ms;
+    }
     return GALP_OK;
 }
 

@@ -204,6 +204,18 @@ struct Engine {
     uint64_t batch_seq = 0;   // running batch counter (buffer parity)
     int64_t h2d_run = 0;      // bytes streamed by the last run
     int64_t launches = 0;     // kernels launched by runs so far (setup excluded)
+    // batched mode: graph g = vertices [g_v0[g], g_v0[g+1]) of the concatenated CSR
+    bool batched = false;
+    int32_t G = 0;
+    int early_exit = 1;
+    int batch_max_iter = 0;   // row length of b_g_counts
+    std::vector<int64_t> g_v0_h;
+    std::vector<int32_t> g_last_h;
+    DevBuf b_g_v0, b_g_base, b_g_last, b_g_active, b_g_iters, b_g_counts;
+    // launch shapes (blocks per SM), chosen by galp_batch_tune
+    int small_bps = 16, mid_bps = 6, resolve_bps = 4;
+    int setup_batch(const galp_csr &g, const int64_t *graph_v0, int32_t count, const galp_opts &o, cudaStream_t st,
+                    int64_t &h2d);
     void launched(const char *name, cudaStream_t st)
     {
         ++launches;
@@ -229,6 +241,9 @@ struct Engine {
 
 struct galp_ctx {
     galp_opts opts{};
+    // batched mode: the whole run captured once per iteration count as a CUDA graph
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_iters = -1;
     int64_t n = 0, m = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;

@@ -74,7 +74,40 @@ struct PipeArgs {
     const uint8_t *dirty;   // 1 = a neighbour's label changed in the previous iteration
     int32_t *changed;       // vertices whose label changes in this iteration
     const DispatchState *disp;  // this iteration's variant (mid-list split, inserts, frontier)
+    // batched mode (null g_v0 = one graph): graph g owns vertices [g_v0[g], g_v0[g+1]), its
+    // own run positions (g_base[g] = run base of its first vertex), labels and last vertex
+    const int64_t *g_v0;
+    const int64_t *g_base;
+    const int32_t *g_last;
+    int32_t ngraphs;
 };
+
+// Graph of vertex v in batched mode: the largest g with g_v0[g] <= v.
+__device__ __forceinline__ int find_graph(const int64_t *g_v0, int ngraphs, int64_t v)
+{
+    int lo = 0, hi = ngraphs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&g_v0[mid]) <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Run position scope of a vertex: its run base a, the scope's run count N, and whether it
+// is the scope's last run-owning vertex (the whole graph, or its graph in batched mode).
+struct RunScope {
+    long long a, N;
+    bool is_last;
+};
+
+__device__ __forceinline__ RunScope run_scope(const PipeArgs &p, int v)
+{
+    if (!p.g_v0) return RunScope{p.runbase[v], p.ctl->N, v == p.last_v};
+    const int g = find_graph(p.g_v0, p.ngraphs, v);
+    const long long base = p.g_base[g];
+    return RunScope{p.runbase[v] - base, p.g_base[g + 1] - base, v == p.g_last[g]};
+}
 
 __device__ __forceinline__ void count_change(unsigned long long &changes, int32_t nl, int32_t old)
 {
@@ -779,9 +812,9 @@ __global__ void __launch_bounds__(kTB) resolve_small_kernel(PipeArgs p)
         const int kw = p.sm_kw[v], rr = p.sm_r[v];
         const int k = kw & 0xFFFF, W = kw >> 16, rmin = rr & 0xFFFF, rmax = rr >> 16;
         const int d = p.dcnt[v];
-        const long long a = p.runbase[v];
-        const long long N = p.ctl->N;
-        const bool is_last = v == p.last_v;
+        const RunScope rs = run_scope(p, v);
+        const long long a = rs.a, N = rs.N;
+        const bool is_last = rs.is_last;
         SummaryQuery q(k, d, rmin, rmax);
         int r = resolve_rank(a, d, N, is_last, q);
         int32_t nl;
@@ -926,9 +959,9 @@ __global__ void __launch_bounds__(kTB) resolve_mid_kernel(PipeArgs p)
         const int kw = p.sm_kw[v], rr = p.sm_r[v];
         const int k = kw & 0xFFFF, W = kw >> 16, rmin = rr & 0xFFFF, rmax = rr >> 16;
         const int d = p.dcnt[v];
-        const long long a = p.runbase[v];
-        const long long N = p.ctl->N;
-        const bool is_last = v == p.last_v;
+        const RunScope rs = run_scope(p, v);
+        const long long a = rs.a, N = rs.N;
+        const bool is_last = rs.is_last;
         SummaryQuery q(k, d, rmin, rmax);
         int r = resolve_rank(a, d, N, is_last, q);
         int32_t nl;
@@ -1003,8 +1036,15 @@ __global__ void __launch_bounds__(kTB) first_iteration_kernel(PipeArgs p, int64_
         int32_t nl = old;
         if (deg > 0) {
             AllCandidates q{deg};
-            const int r = resolve_rank(o0, deg, m, v == p.last_v, q);
-            nl = __ldg(&p.nbr[o0 + r]);
+            if (!p.g_v0) {
+                const int r = resolve_rank(o0, deg, m, v == p.last_v, q);
+                nl = __ldg(&p.nbr[o0 + r]);
+            } else {  // graph-local run positions and labels
+                const int g = find_graph(p.g_v0, p.ngraphs, v);
+                const int64_t vg = p.g_v0[g], e0 = __ldg(&p.off[vg]), e1 = __ldg(&p.off[p.g_v0[g + 1]]);
+                const int r = resolve_rank(o0 - e0, deg, e1 - e0, v == p.g_last[g], q);
+                nl = (int32_t)(__ldg(&p.nbr[o0 + r]) - vg);
+            }
         }
         p.lab_out[v] = nl;
         p.dcnt[v] = (int32_t)deg;  // every neighbour label distinct (insert-aggregation hint)
@@ -1075,6 +1115,106 @@ __global__ void __launch_bounds__(kTB) adjacency_check_kernel(const int64_t *off
         if (desc) atomicAdd(&out[0], desc);
         atomicAdd(&out[1], s1);
         atomicAdd(&out[2], s2);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// batched mode: many independent graphs in one concatenated CSR
+// ---------------------------------------------------------------------------
+
+// Initial labels: graph-local vertex IDs.  One block per graph (grid-stride).
+// Sets *bad when an edge leaves its graph.  One block per graph (grid-stride).
+__global__ void __launch_bounds__(kTB) batch_validate_kernel(const int64_t *off, const int32_t *nbr,
+                                                             const int64_t *g_v0, int ngraphs, int *bad)
+{
+    for (int g = blockIdx.x; g < ngraphs; g += gridDim.x) {
+        const int64_t v0 = g_v0[g], v1 = g_v0[g + 1];
+        int b = 0;
+        for (int64_t e = off[v0] + threadIdx.x; e < off[v1]; e += blockDim.x) {
+            const int64_t u = nbr[e];
+            b |= (u < v0 || u >= v1);
+        }
+        if (__any_sync(kFull, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+    }
+}
+
+__global__ void __launch_bounds__(kTB) batch_init_labels_kernel(const int64_t *g_v0, int ngraphs, int32_t *lab)
+{
+    for (int g = blockIdx.x; g < ngraphs; g += gridDim.x) {
+        const int64_t v0 = g_v0[g], v1 = g_v0[g + 1];
+        for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) lab[v] = (int32_t)(v - v0);
+    }
+}
+
+// Per-graph run bases after the scan: g_base[g] = run base of graph g's first vertex,
+// g_base[ngraphs] = all runs.
+__global__ void batch_bases_kernel(const int64_t *g_v0, int ngraphs, const int64_t *runbase, int64_t n, const Ctl *ctl,
+                                   int64_t *g_base)
+{
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g <= ngraphs; g += gridDim.x * blockDim.x) {
+        const int64_t v = g_v0[g];
+        g_base[g] = v < n ? runbase[v] : ctl->N;
+    }
+}
+
+// After an iteration: per graph, the labels that changed and the reference's early exit
+// (count <= n_g * 1e-5, dpp.cuh:88) per graph.  A graph that had already exited keeps its
+// labels (lab_out = lab_in).  One block per graph (grid-stride).
+__global__ void __launch_bounds__(kTB) batch_commit_kernel(const Ctl *ctl, const int64_t *g_v0, int ngraphs,
+                                                           const int32_t *lab_in, int32_t *lab_out, int32_t *g_active,
+                                                           int32_t *g_iters, long long *g_counts, int max_iter, int it,
+                                                           int early_exit)
+{
+    __shared__ unsigned long long part[kTB / 32];
+    if (!ctl_active(ctl)) return;  // every graph exited earlier: the final buffer is settled
+    for (int g = blockIdx.x; g < ngraphs; g += gridDim.x) {
+        const int64_t v0 = g_v0[g], v1 = g_v0[g + 1];
+        if (!g_active[g]) {
+            for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) lab_out[v] = lab_in[v];
+            continue;
+        }
+        unsigned long long c = 0;
+        for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) c += lab_out[v] != lab_in[v];
+        c = __reduce_add_sync(kFull, (unsigned)c);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < kTB / 32; ++w) t += part[w];
+            if (it < max_iter) g_counts[(int64_t)g * max_iter + it] = (long long)t;
+            g_iters[g] = it + 1;
+            if ((early_exit && (double)t <= (double)(v1 - v0) * 1e-5) || it + 1 >= max_iter) g_active[g] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+// Global bookkeeping after batch_commit: the run goes on while some graph is active.
+__global__ void batch_finalize_kernel(Ctl *ctl, const int32_t *g_active, int ngraphs)
+{
+    __shared__ int any;
+    if (threadIdx.x == 0) any = 0;
+    __syncthreads();
+    for (int g = threadIdx.x; g < ngraphs; g += blockDim.x)
+        if (g_active[g]) any = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (ctl->active) {
+            const unsigned long long c = ctl->changes;
+            if (ctl->iter < 64) ctl->counts[ctl->iter] = c;
+            ctl->iter += 1;
+            if (!any || ctl->iter >= ctl->max_iter) ctl->active = 0;
+        }
+        ctl->changes = 0;
+        ctl->ticket = 0;
+    }
+}
+
+__global__ void batch_init_kernel(int32_t *g_active, int32_t *g_iters, int ngraphs, int active)
+{
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngraphs; g += gridDim.x * blockDim.x) {
+        g_active[g] = active;
+        g_iters[g] = 0;
     }
 }
 

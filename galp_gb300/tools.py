@@ -274,3 +274,22 @@ class MLP:
         if rc:
             raise RuntimeError(f"galp_mlp_train: {rc}")
         return curve[:steps]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("small_blocks_per_sm", ctypes.c_int32), ("mid_blocks_per_sm", ctypes.c_int32),
+                ("resolve_blocks_per_sm", ctypes.c_int32), ("trials", ctypes.c_int32), ("best_ms", ctypes.c_float),
+                ("pad", ctypes.c_int32)]
+
+
+def batch_tune(batch, niter: int = 3) -> dict:
+    """Launch-shape autotuner of a batched context (galp_batch_tune)."""
+    L = _lib()
+    L.galp_batch_tune.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(TuneResult)]
+    L.galp_batch_tune.restype = ctypes.c_int
+    r = TuneResult()
+    rc = L.galp_batch_tune(batch._h, niter, ctypes.byref(r))
+    if rc:
+        raise RuntimeError(f"galp_batch_tune: {rc}")
+    return dict(small_blocks_per_sm=r.small_blocks_per_sm, mid_blocks_per_sm=r.mid_blocks_per_sm,
+                resolve_blocks_per_sm=r.resolve_blocks_per_sm, trials=r.trials, best_ms=r.best_ms)

@@ -13,6 +13,7 @@
  *   galp_get_labels  LabelPropagator::get_labels() (include/label_propagator.h:25-29)
  *   galp_destroy     postprocess() + destructor (src/common/incore.cuh:51-55)
  *   galp_run_batch   no reference counterpart: clusters many independent graphs
+ *                    (galp_batch_create/_stats/_labels for the same as a context)
  *
  * All arguments are plain pointers and sizes.  The library never calls exit();
  * every entry point returns a status (0 = OK, negative = error, see galp_strerror).
@@ -126,6 +127,26 @@ int galp_sync(galp_ctx *ctx, galp_stats *stats);
 #define GALP_NOALLOC_MAX_ENTRIES (1 << 21)
 int galp_run_noalloc(const galp_csr *graph, int32_t niter, int32_t early_exit, int32_t *labels_out,
                      galp_stats *stats, void *stream);
+
+/* Batched mode (no counterpart in the reference): many independent graphs clustered
+ * together, each with exactly the labels, iteration count and change counts of its own
+ * in-core run (policy 0): labels start at graph-local IDs, run positions and the early
+ * exit are per graph, and a graph that has exited keeps its labels while the others go
+ * on.  A run is one CUDA-graph launch.  Vertices above 12288 neighbours are not
+ * supported here (GALP_EUNSUPPORTED).
+ *
+ * galp_run_batch: one call over `count` host graphs; labels_out = int32[sum of n] in
+ * graph order (graph-local labels), stats = galp_stats[count] or NULL. */
+int galp_run_batch(const galp_csr *graphs, int32_t count, const galp_opts *opts, int32_t niter,
+                   int32_t *labels_out, galp_stats *stats);
+/* The batch as a context: one concatenated CSR (offsets int64[n+1], neighbours with
+ * global IDs, host or device pointers), graph g = vertices [graph_v0[g],
+ * graph_v0[g+1]) (host array of count+1), no edge leaving its graph.  Run it with
+ * galp_run / galp_enqueue; read per-graph results with the two calls below. */
+int galp_batch_create(const int64_t *offsets, const int32_t *neighbors, int64_t n, int64_t m,
+                      const int64_t *graph_v0, int32_t count, const galp_opts *opts, galp_ctx **out);
+int galp_batch_stats(galp_ctx *ctx, int32_t graph, galp_stats *stats);
+int galp_batch_labels(galp_ctx *ctx, int32_t graph, int32_t *labels, int64_t n);
 
 /* Host-side evaluation of the tie-break closed form, for tests: winning candidate
  * rank of a vertex with run base a, distinct count d, in a scope of N runs, given

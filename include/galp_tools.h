@@ -72,7 +72,16 @@ typedef struct {
 #define GALP_DISPATCH_HIDDEN 64
 #define GALP_DISPATCH_VARIANTS 16
 
+typedef struct {
+    int32_t small_blocks_per_sm, mid_blocks_per_sm, resolve_blocks_per_sm, trials;
+    float best_ms;         /* probe run time with the chosen shapes */
+    int32_t pad;
+} galp_tune_result;
+
 int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info);
+/* Launch-shape autotuner of a batched context (galp_batch_create): times probe runs of
+ * niter iterations and keeps the fastest blocks-per-SM of the counting/resolve kernels. */
+int galp_batch_tune(galp_ctx *ctx, int32_t niter, galp_tune_result *res);
 
 /* Per-iteration dispatch: mode 0 = fixed rule (default), 1 = learned MLP (weights: the
  * galp_mlp_size(24, 64, 16) parameters of a galp_mlp, or NULL to keep those loaded; the

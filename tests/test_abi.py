@@ -18,8 +18,8 @@ def _declared(header):
     return sorted(set(re.findall(r"\b(galp_[a-z0-9_]+)\s*\(", txt)))
 
 
-@pytest.mark.parametrize("header,lib", [("galp.h", "libgalp.so"), ("galp_gen.h", "libgalp_gen.so"),
-                                        ("galp_host.h", "libgalp_host.so")])
+@pytest.mark.parametrize("header,lib", [("galp.h", "libgalp.so"), ("galp_tools.h", "libgalp.so"),
+                                        ("galp_gen.h", "libgalp_gen.so"), ("galp_host.h", "libgalp_host.so")])
 def test_library_exports_every_declared_symbol(header, lib):
     if not os.path.exists(os.path.join(ROOT, "include", header)):
         pytest.skip(f"{header} not present")
