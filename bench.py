@@ -184,7 +184,7 @@ def run_batch(args, desc_count: int):
     b = galp_gb300.Batch(offsets=off_d.data_ptr(), neighbors=nbr_d.data_ptr(), graph_v0=v0, n=n, m=m)
     setup_s = time.perf_counter() - t0
     b.set_stream(stream.cuda_stream)
-    tune = b.tune(3)
+    tune = b.tune(NITER)
     for _ in range(args.warmup):
         b.enqueue(NITER)
     b.sync()
@@ -439,6 +439,7 @@ def run_gpu(args, g, desc, rank, world, dist):
         dist.barrier()
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = tools.schedule_info(p).launches
     with ClockSampler(dev) as clk:
         ev0.record(stream)
         for _ in range(args.steps):
@@ -447,6 +448,7 @@ def run_gpu(args, g, desc, rank, world, dist):
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     st = p.sync()
+    launches_timed = tools.schedule_info(p).launches - launches0
     kt = tools.profile_read(p)
     if st.err:
         raise RuntimeError(f"device error bits {st.err}")
@@ -484,6 +486,35 @@ def run_gpu(args, g, desc, rank, world, dist):
     p.close()
     del p
 
+    # frontier mode under the fixed rule and the learned dispatcher (same labels)
+    dispatch = None
+    if not args.no_dispatch:
+        dispatch = {"frontier": True, "iterations": NITER}
+        for name, kw in (("fixed", {}), ("learned", {"dispatch": 1})):
+            try:
+                q = galp_gb300.Propagator(g, early_exit=0, frontier=1, device=dev, **kw)
+            except galp_gb300.GalpError as e:
+                dispatch[name] = f"unavailable: {e}"
+                continue
+            q.set_stream(stream.cuda_stream)
+            for _ in range(args.warmup):
+                q.enqueue(NITER)
+            q.sync()
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                q.enqueue(NITER)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            dispatch[name + "_ms_per_iter"] = round(ev0.elapsed_time(ev1) / args.steps / NITER, 4)
+            dispatch[name + "_rows"] = [int(r) for r in tools.dispatch_log(q)[1]]
+            q.close()
+        if "fixed_ms_per_iter" in dispatch and "learned_ms_per_iter" in dispatch:
+            dispatch["learned_speedup_vs_fixed"] = round(dispatch["fixed_ms_per_iter"] /
+                                                         dispatch["learned_ms_per_iter"], 3)
+        if "fixed_ms_per_iter" in dispatch:
+            dispatch["frontier_fixed_vs_dense"] = round((ms_per_step / NITER) / dispatch["fixed_ms_per_iter"], 3)
+
     # end-to-end arm through the C ABI with host buffers
     e2e_times = []
     h2d = d2h = 0
@@ -514,7 +545,6 @@ def run_gpu(args, g, desc, rank, world, dist):
                "kind": "port",
                "sample": (f"one sweep of CPUWorker::update_label (port) over vertices [0, {s['vertices']}) = "
                           f"{s['edges']} of {g.m} CSR entries, OpenMP dynamic schedule")}
-    launches_step = 2 + 2 + NITER * info.launches_per_iter  # init labels/ctl + per-iteration kernels
     cfg = dict(desc)
     cfg.update(iterations_per_step=NITER, early_exit=False, method=0, policy=0,
                l2="inputs larger than L2 (neighbours {:.1f} GB vs 129 MB L2)".format(4 * g.m / 1e9),
@@ -529,7 +559,8 @@ def run_gpu(args, g, desc, rank, world, dist):
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_val, 3) if e2e_val else None, "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_t, 4)},
-        "gpu_launches": int(launches_step * args.steps),
+        "dispatch": dispatch,
+        "gpu_launches": int(launches_timed),
         "iteration_ms": round(ms_per_step / NITER, 4),
     }
     return line
@@ -545,6 +576,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-dispatch", action="store_true")
     args = ap.parse_args()
     rank, world, local = _rank_env()
 

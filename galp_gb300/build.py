@@ -51,7 +51,7 @@ def _deps(*dirs: str) -> list[str]:
         for base, _, files in os.walk(d):
             if "_ref" in base or "_build" in base or "lib" == os.path.basename(base):
                 continue
-            out += [os.path.join(base, f) for f in files if f.endswith((".cu", ".cuh", ".h", ".cpp", ".c"))]
+            out += [os.path.join(base, f) for f in files if f.endswith((".cu", ".cuh", ".h", ".inc", ".cpp", ".c"))]
     return out
 
 

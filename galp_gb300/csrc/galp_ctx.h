@@ -197,7 +197,7 @@ struct Engine {
     bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
     bool symmetric = false;   // edge multiset symmetric (frontier marking along out-edges)
     Profiler prof;
-    galp_variant variant{2, 0.05f, 0.03f, {}};  // kernel variant knobs (galp_set_variant)
+    galp_variant variant{2, 0.05f, 0.03f, 0, {}};  // kernel variant knobs (galp_set_variant)
     // out-of-core streaming
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
@@ -211,7 +211,8 @@ struct Engine {
     int batch_max_iter = 0;   // row length of b_g_counts
     std::vector<int64_t> g_v0_h;
     std::vector<int32_t> g_last_h;
-    DevBuf b_g_v0, b_g_base, b_g_last, b_g_active, b_g_iters, b_g_counts;
+    DevBuf b_g_v0, b_g_base, b_g_last, b_g_active, b_g_iters, b_g_counts, b_gid;
+    int64_t max_label = 0;    // labels stay below this (n, or the largest graph of a batch)
     // launch shapes (blocks per SM), chosen by galp_batch_tune
     int small_bps = 16, mid_bps = 6, resolve_bps = 4;
     int setup_batch(const galp_csr &g, const int64_t *graph_v0, int32_t count, const galp_opts &o, cudaStream_t st,

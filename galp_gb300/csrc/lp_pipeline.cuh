@@ -79,7 +79,10 @@ struct PipeArgs {
     const int64_t *g_v0;
     const int64_t *g_base;
     const int32_t *g_last;
+    const int32_t *gid;     // graph of every vertex
     int32_t ngraphs;
+    int32_t lab27;          // every label below 2^27 - 1 (32-bit sort keys in packs)
+    int32_t small_sort;     // small packs: sort-based counting (needs lab27) instead of match_any
 };
 
 // Graph of vertex v in batched mode: the largest g with g_v0[g] <= v.
@@ -104,7 +107,7 @@ struct RunScope {
 __device__ __forceinline__ RunScope run_scope(const PipeArgs &p, int v)
 {
     if (!p.g_v0) return RunScope{p.runbase[v], p.ctl->N, v == p.last_v};
-    const int g = find_graph(p.g_v0, p.ngraphs, v);
+    const int g = __ldg(&p.gid[v]);
     const long long base = p.g_base[g];
     return RunScope{p.runbase[v] - base, p.g_base[g + 1] - base, v == p.g_last[g]};
 }
@@ -152,10 +155,48 @@ __device__ __forceinline__ void warp_note_changes(const PipeArgs &p, bool change
     if (p.changed) warp_append(changed, v, p.changed, &p.ctl->changed_n);
 }
 
+// Per-vertex results of a counted pack: the values live at each vertex's first slot lane
+// and move to the vertex lanes, which write the vertex state (all lanes call this).
+__device__ __forceinline__ void finish_small_pack(const PipeArgs &p, bool vl, int v, int deg, int pos, int d, int k,
+                                                  int W, int cmin, int cmax, int rmin, int rmax,
+                                                  unsigned long long &changes)
+{
+    const int lane = threadIdx.x & 31;
+    // results live at each vertex's first slot lane; bring them to the vertex lanes
+    const int src = (vl && deg > 0) ? pos : lane;
+    // d, k, W <= 32 and ranks < 32: one word
+    const uint32_t packed = (uint32_t)d | ((uint32_t)k << 6) | ((uint32_t)W << 12) | ((uint32_t)rmin << 18) |
+                            ((uint32_t)rmax << 23);
+    const uint32_t pk_v = __shfl_sync(kFull, packed, src);
+    const int d_v = (int)(pk_v & 63), k_v = (int)((pk_v >> 6) & 63), W_v = (int)((pk_v >> 12) & 63);
+    const int r0_v = (int)((pk_v >> 18) & 31), r1_v = (int)((pk_v >> 23) & 31);
+    const int c0_v = __shfl_sync(kFull, cmin, src);
+    const int c1_v = __shfl_sync(kFull, cmax, src);
+    const bool tied = vl && deg > 0 && k_v > 1;
+    bool chg = false;
+    if (vl) {
+        p.dcnt[v] = deg > 0 ? d_v : 0;
+        const int32_t old = __ldg(&p.lab_in[v]);
+        if (deg > 0) p.sm_kw[v] = k_v | (W_v << 16);
+        if (!tied) {
+            const int32_t nl = deg > 0 ? c0_v : old;
+            p.lab_out[v] = nl;
+            count_change(changes, nl, old);
+            chg = nl != old;
+        } else {
+            p.sm_c0[v] = c0_v;
+            p.sm_c1[v] = c1_v;
+            p.sm_r[v] = r0_v | (r1_v << 16);
+        }
+    }
+    warp_append(tied, v, p.tied_small, &p.ctl->tied_small);
+    warp_note_changes(p, chg, v);
+}
+
 // ---------------------------------------------------------------------------
 // small vertices: one warp per pack
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
+__global__ void __launch_bounds__(256, 6) count_small_kernel(PipeArgs p)
 {
     if (!ctl_active(p.ctl)) return;
     const bool fr = frontier_on(p);
@@ -177,36 +218,64 @@ __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
             warp_append(tied, v, p.tied_small, &p.ctl->tied_small);
             continue;
         }
-        const int64_t o0 = vl ? __ldg(&p.off[v]) : 0;
-        const int deg = vl ? (int)(__ldg(&p.off[v + 1]) - o0) : 0;
-        int pos = deg;
-#pragma unroll
-        for (int s = 1; s < 32; s <<= 1) {
-            const int o = __shfl_up_sync(kFull, pos, s);
-            if (lane >= s) pos += o;
-        }
-        const int total = __shfl_sync(kFull, pos, 31);
-        pos -= deg;  // exclusive
-        // slot lanes: owner vertex lane j, CSR entry, label
+        // The pack's CSR entries are contiguous: slot lane i holds entry obase + i.  Vertex
+        // lanes read their offsets (an offset minus obase is the vertex's first slot lane);
+        // the slot lanes of one vertex form a segment [first, last] found from the mask of
+        // segment starts.
+        const int64_t ol = __ldg(&p.off[v0 + min(lane, nv)]);
+        const int64_t obase = __shfl_sync(kFull, ol, 0);
+        const int64_t oend = nv < 32 ? __shfl_sync(kFull, ol, nv) : __ldg(&p.off[v0 + 32]);
+        const int64_t onext = __shfl_down_sync(kFull, ol, 1);
+        const int deg = vl ? (int)((lane == 31 ? oend : onext) - ol) : 0;
+        const int pos = (int)(ol - obase);
+        const int total = (int)(oend - obase);
         const bool valid = lane < total;
-        // owner of slot `lane`: the last vertex lane whose first slot is <= lane
-        // (positions are non-decreasing over the vertex lanes; binary lifting)
-        int j = 0;
-#pragma unroll
-        for (int step = 16; step > 0; step >>= 1) {
-            const int t = j + step;
-            const int pt = __shfl_sync(kFull, pos, t < 32 ? t : 31);
-            if (t < nv && pt <= lane) j = t;
-        }
-        if (!valid) j = 0;
-        const int64_t oj = __shfl_sync(kFull, o0, j);
-        const int pj = __shfl_sync(kFull, pos, j);
+        const unsigned starts = __reduce_or_sync(kFull, (vl && deg > 0) ? (1u << pos) : 0u);
+        const unsigned upto = (2u << lane) - 1u;  // lanes 0..lane
+        const int j = valid ? 31 - __clz(starts & upto) : lane;  // segment id = its first lane
+        const unsigned later_start = starts & ~upto;
+        const int seg_last = valid ? (later_start ? __ffs(later_start) - 2 : total - 1) : lane;
+        const int64_t oj = obase + j;  // the owner's first CSR entry
         int lab = 0;
-        if (valid) lab = __ldg(&p.lab_in[__ldg(&p.nbr[oj + (lane - pj) - p.nbr_shift])]);
-        // count in registers: the slot lanes of vertex j are [pj, pj + deg_j)
-        const int dj = __shfl_sync(kFull, deg, j);
-        const unsigned vm = valid ? (((pj + dj >= 32) ? kFull : ((1u << (pj + dj)) - 1)) & ~((1u << pj) - 1))
+        if (valid) lab = __ldg(&p.lab_in[__ldg(&p.nbr[obase + lane - p.nbr_shift])]);
+        const unsigned vm = valid ? (((seg_last == 31) ? kFull : ((2u << seg_last) - 1u)) & ~((1u << j) - 1u))
                                   : (1u << lane);
+        if (p.small_sort && p.lab27) {
+            // Sort-based counting: sort the pack by (vertex lane << 27 | label) in one 32-bit
+            // key (padding lanes last; a vertex keeps its slot lanes), then every run of equal
+            // keys is one distinct label: heads give d, run lengths give counts, and
+            // candidates come out in label order (cmin/cmax and their ranks by bit scans).
+            uint32_t sk = valid ? (((uint32_t)j << 27) | (uint32_t)lab) : 0xFFFFFFFFu;
+#pragma unroll
+            for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                    const uint32_t ok = __shfl_xor_sync(kFull, sk, jj);
+                    const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
+                    sk = ((lower == up) ? (ok < sk) : (ok > sk)) ? ok : sk;
+                }
+            }
+            const int first = __ffs(vm) - 1, last = 31 - __clz(vm);
+            const int slab = (int)(sk & ((1u << 27) - 1));
+            const uint32_t prevk = __shfl_up_sync(kFull, sk, 1);
+            const bool head = valid && (lane == first || prevk != sk);
+            const unsigned hm = __ballot_sync(kFull, head) & vm;
+            const unsigned later = hm & ~((2u << lane) - 1u);
+            const int cnt = head ? (later ? __ffs(later) - 1 : last + 1) - lane : 0;
+            const int W = seg_max(cnt, lane, first, last);
+            const unsigned cm = __ballot_sync(kFull, head && cnt == W) & vm;
+            const int k = __popc(cm), d = __popc(hm);
+            const int lo = cm ? __ffs(cm) - 1 : lane, hi = cm ? 31 - __clz(cm) : lane;
+            const int cmin = __shfl_sync(kFull, slab, lo), cmax = __shfl_sync(kFull, slab, hi);
+            const int rmin = __popc(hm & ((1u << lo) - 1)), rmax = __popc(hm & ((1u << hi) - 1));
+            if (head && k > 2) {
+                const int64_t e = oj - p.nbr_shift + __popc(hm & ((1u << lane) - 1));
+                p.run_lab[e] = slab;
+                p.run_cnt[e] = (uint16_t)cnt;
+            }
+            finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes);
+            continue;
+        }
         const unsigned eq = __match_any_sync(kFull, valid ? (uint32_t)lab : (0x80000000u | (uint32_t)lane)) & vm;
         const int cnt = __popc(eq);
         const bool leader = valid && ((__ffs(eq) - 1) == lane);
@@ -226,9 +295,35 @@ __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
             cmax = seg_max(cand ? lab : -1, lane, first, last);
             rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
             rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
-            if (__any_sync(kFull, valid && k > 2)) {
+            if (p.lab27 && __any_sync(kFull, valid && k > 2)) {
                 // resolving a vertex with more than two candidates may need its runs in
-                // label order: sort the pack by (vertex, label) and spill those runs
+                // label order: sort the pack by (vertex lane << 27 | label) in one 32-bit
+                // key (labels below 2^27 - 1; padding lanes sort last), then spill the
+                // runs of those vertices; run lengths come from the run heads
+                uint32_t sk = valid ? (((uint32_t)j << 27) | (uint32_t)lab) : 0xFFFFFFFFu;
+#pragma unroll
+                for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+                    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                        const uint32_t ok = __shfl_xor_sync(kFull, sk, jj);
+                        const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
+                        sk = ((lower == up) ? (ok < sk) : (ok > sk)) ? ok : sk;
+                    }
+                }
+                const int slab = (int)(sk & ((1u << 27) - 1));
+                const uint32_t prevk = __shfl_up_sync(kFull, sk, 1);
+                const bool head = valid && (lane == first || prevk != sk);
+                const unsigned hm = __ballot_sync(kFull, head) & vm;
+                const int rank = __popc(hm & ((1u << lane) - 1));
+                const unsigned later = hm & ~((2u << lane) - 1u);
+                const int sc = (later ? __ffs(later) - 1 : last + 1) - lane;
+                if (head && k > 2) {
+                    const int64_t e = oj - p.nbr_shift + rank;
+                    p.run_lab[e] = slab;
+                    p.run_cnt[e] = (uint16_t)sc;
+                }
+            } else if (__any_sync(kFull, valid && k > 2)) {
+                // labels of 27 bits or more: 64-bit (vertex, label) keys
                 unsigned long long sk =
                     valid ? (((unsigned long long)(unsigned)j << 32) | (unsigned)lab) : (0xFFFFFFFF00000000ull | lane);
                 int sc = valid ? cnt : 0;
@@ -257,34 +352,7 @@ __global__ void __launch_bounds__(256) count_small_kernel(PipeArgs p)
                 }
             }
         }
-        // results live at each vertex's first slot lane; bring them to the vertex lanes
-        const int src = (vl && deg > 0) ? pos : lane;
-        const int d_v = __shfl_sync(kFull, d, src);
-        const int k_v = __shfl_sync(kFull, k, src);
-        const int W_v = __shfl_sync(kFull, W, src);
-        const int c0_v = __shfl_sync(kFull, cmin, src);
-        const int c1_v = __shfl_sync(kFull, cmax, src);
-        const int r0_v = __shfl_sync(kFull, rmin, src);
-        const int r1_v = __shfl_sync(kFull, rmax, src);
-        const bool tied = vl && deg > 0 && k_v > 1;
-        bool chg = false;
-        if (vl) {
-            p.dcnt[v] = deg > 0 ? d_v : 0;
-            const int32_t old = __ldg(&p.lab_in[v]);
-            if (deg > 0) p.sm_kw[v] = k_v | (W_v << 16);
-            if (!tied) {
-                const int32_t nl = deg > 0 ? c0_v : old;
-                p.lab_out[v] = nl;
-                count_change(changes, nl, old);
-                chg = nl != old;
-            } else {
-                p.sm_c0[v] = c0_v;
-                p.sm_c1[v] = c1_v;
-                p.sm_r[v] = r0_v | (r1_v << 16);
-            }
-        }
-        warp_append(tied, v, p.tied_small, &p.ctl->tied_small);
-        warp_note_changes(p, chg, v);
+        finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes);
     }
     flush_changes(changes, p.ctl);
 }
@@ -1040,7 +1108,7 @@ __global__ void __launch_bounds__(kTB) first_iteration_kernel(PipeArgs p, int64_
                 const int r = resolve_rank(o0, deg, m, v == p.last_v, q);
                 nl = __ldg(&p.nbr[o0 + r]);
             } else {  // graph-local run positions and labels
-                const int g = find_graph(p.g_v0, p.ngraphs, v);
+                const int g = __ldg(&p.gid[v]);
                 const int64_t vg = p.g_v0[g], e0 = __ldg(&p.off[vg]), e1 = __ldg(&p.off[p.g_v0[g + 1]]);
                 const int r = resolve_rank(o0 - e0, deg, e1 - e0, v == p.g_last[g], q);
                 nl = (int32_t)(__ldg(&p.nbr[o0 + r]) - vg);
@@ -1121,6 +1189,13 @@ __global__ void __launch_bounds__(kTB) adjacency_check_kernel(const int64_t *off
 // ---------------------------------------------------------------------------
 // batched mode: many independent graphs in one concatenated CSR
 // ---------------------------------------------------------------------------
+
+// Graph of every vertex (set up once).  One block per graph (grid-stride).
+__global__ void __launch_bounds__(kTB) batch_gid_kernel(const int64_t *g_v0, int ngraphs, int32_t *gid)
+{
+    for (int g = blockIdx.x; g < ngraphs; g += gridDim.x)
+        for (int64_t v = g_v0[g] + threadIdx.x; v < g_v0[g + 1]; v += blockDim.x) gid[v] = g;
+}
 
 // Initial labels: graph-local vertex IDs.  One block per graph (grid-stride).
 // Sets *bad when an edge leaves its graph.  One block per graph (grid-stride).

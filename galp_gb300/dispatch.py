@@ -36,18 +36,22 @@ WEIGHTS_INC = os.path.join(HERE, "csrc", "dispatch_weights.inc")
 
 def training_graphs(seed: int = 7):
     """Seeded training set: R-MAT of several scales, edge factors and skews, planted
-    partitions and LFR-style graphs (sizes that generate in seconds on the host)."""
+    partitions and LFR-style graphs of several mixings (sizes that generate in seconds
+    on the host)."""
     specs = []
-    for scale, ef, a in [(16, 8, 0.57), (17, 16, 0.57), (18, 16, 0.57), (18, 32, 0.45), (19, 8, 0.45),
-                         (19, 16, 0.57), (20, 16, 0.57), (20, 8, 0.50), (21, 4, 0.57)]:
-        b = c = (1 - a) / 3 if a < 0.57 else 0.19
+    rmats = [(16, 8, 0.57), (17, 16, 0.57), (18, 16, 0.57), (18, 32, 0.45), (19, 8, 0.45), (19, 16, 0.57),
+             (20, 16, 0.57), (20, 8, 0.50), (21, 4, 0.57), (17, 32, 0.65), (18, 8, 0.65), (19, 32, 0.50),
+             (20, 32, 0.57), (21, 16, 0.57), (21, 8, 0.45), (22, 8, 0.57), (22, 16, 0.50), (16, 64, 0.57)]
+    for scale, ef, a in rmats:
+        b = c = (1 - a) / 3 if a < 0.57 else (1 - a) / 2.27
         specs.append((f"rmat{scale}-ef{ef}-a{a}", lambda s=scale, e=ef, a=a, b=b, c=c: generate_rmat(s, e, a, b, c,
                                                                                                      seed=seed)))
-    for nb, bs, din, dout in [(64, 256, 16.0, 2.0), (256, 512, 12.0, 3.0), (32, 4096, 24.0, 6.0)]:
+    for nb, bs, din, dout in [(64, 256, 16.0, 2.0), (256, 512, 12.0, 3.0), (32, 4096, 24.0, 6.0),
+                              (1024, 128, 8.0, 4.0), (16, 16384, 20.0, 2.0)]:
         specs.append((f"sbm{nb}x{bs}", lambda nb=nb, bs=bs, din=din, dout=dout: generate_sbm([bs] * nb, din, dout,
                                                                                              seed=seed)))
-    for n in (200_000, 600_000):
-        specs.append((f"lfr{n}", lambda n=n: generate_lfr(n, seed=seed)))
+    for n, mu in [(200_000, 0.3), (600_000, 0.3), (400_000, 0.1), (400_000, 0.5)]:
+        specs.append((f"lfr{n}-mu{mu}", lambda n=n, mu=mu: generate_lfr(n, mu=mu, seed=seed)))
     return specs
 
 
@@ -124,7 +128,7 @@ def predict_rows(w, X, margin: float = 0.03):
 
 def export_inc(w, path: str = WEIGHTS_INC):
     """Write the trained weights as the library's built-in learned dispatcher."""
-    body = ",\n".join(", ".join(f"{x:.9g}f" for x in w[i:i + 8]) for i in range(0, len(w), 8))
+    body = ",\n".join(", ".join(f"{x:.9e}f" for x in w[i:i + 8]) for i in range(0, len(w), 8))
     with open(path, "w") as fh:
         fh.write("// Trained dispatcher weights (galp_mlp layout, 24 -> 64 -> 64 -> 16), written by\n"
                  "// galp_gb300/dispatch.py from timing sweeps on GB300.\n"

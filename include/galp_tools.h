@@ -56,7 +56,8 @@ typedef struct {
                               of labels changed recounts every vertex (default 0.05) */
     float learned_margin;  /* learned rule: predicted log gain needed to leave the fixed rule's
                               choice (default 0.03) */
-    int32_t pad[5];
+    int32_t small_sort;    /* packs of small vertices: 1 = sort-based counting, 0 = match-based */
+    int32_t pad[4];
 } galp_variant;
 
 /* One row of the in-core variant table (every row computes the same labels). */

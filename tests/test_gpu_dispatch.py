@@ -101,3 +101,28 @@ def test_dispatch_set_validates():
             tools.dispatch_set(p, 2, 16)
         with pytest.raises(RuntimeError):
             tools.dispatch_set(p, 1, 0, np.zeros(5, np.float32))
+
+
+def test_builtin_learned_dispatch_is_exact_and_not_slower():
+    """opts.dispatch = 1 loads the network trained on this machine's timing sweeps; it
+    changes only speed.  Per-iteration device time against the fixed rule is printed;
+    the bound allows run-to-run noise."""
+    g = galp_gb300.generate_rmat(19, 32, a=0.5, b=0.1667, c=0.1667, seed=9)
+    times = {}
+    labels = {}
+    for name, kw in (("fixed", {}), ("learned", {"dispatch": 1})):
+        with galp_gb300.Propagator(g, frontier=1, early_exit=0, **kw) as p:
+            p.run(10)
+            tools.profile(p, 1)
+            tools.profile_iterations(p)
+            best = None
+            for _ in range(3):
+                p.run(10)
+                ms = tools.profile_iterations(p)
+                best = ms if best is None else np.minimum(best, ms)
+            times[name] = float(best.sum())
+            labels[name] = p.get_labels()
+    assert np.array_equal(labels["fixed"], labels["learned"])
+    print(f"fixed {times['fixed']:.3f} ms, learned {times['learned']:.3f} ms, "
+          f"gain {times['fixed'] / times['learned']:.3f}x")
+    assert times["learned"] <= 1.10 * times["fixed"]

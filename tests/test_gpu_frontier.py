@@ -157,3 +157,16 @@ def test_insert_aggregation_variants(agg):
         got, its = p.get_labels(), p.iters_run
     it, want, counts = oracle.run(g.offsets, g.neighbors, 6)
     assert its == it and np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("small_sort", [0, 1])
+def test_small_pack_counting_variants(small_sort):
+    # sort-based and match-based counting of small-vertex packs give the same labels
+    for g in (galp_gb300.generate_rmat(16, 8, seed=6), galp_gb300.generate_lfr(20000, seed=8),
+              galp_gb300.generate_sbm([128] * 32, 10.0, 3.0, seed=2)):
+        with galp_gb300.Propagator(g) as p:
+            tools.set_variant(p, small_sort=small_sort)
+            p.run(10)
+            got, its, upd = p.get_labels(), p.iters_run, list(p.updates)
+        it, want, counts = oracle.run(g.offsets, g.neighbors, 10)
+        assert its == it and upd == list(counts) and np.array_equal(got, want)
