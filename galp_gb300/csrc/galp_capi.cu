@@ -16,6 +16,7 @@
 #include <cstring>
 #include <memory>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "../../include/galp.h"
@@ -51,15 +52,68 @@ int cuda_status(cudaError_t e)
         if (e_ != cudaSuccess) return cuda_status(e_);     \
     } while (0)
 
-// Static per-graph schedule (host), per scope: packs of consecutive vertices of
-// degree <= 32 (at most 32 vertices and 32 edges; a pack ends at a vertex of another
-// bucket), mid (33..256) and large (257..2048) vertex lists, and big vertices (> 2048)
-// with global hash tables (offsets relative to the scope, so out-of-core batches reuse
-// one table area) and their work chunks.
-void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts)
+namespace {
+
+// One thread's share of a scope: packs, mid-list vertices (unsorted), big vertices.
+struct ChunkPlan {
+    std::vector<int32_t> pack_v0;
+    std::vector<uint8_t> pack_nv;
+    std::vector<int32_t> mid;
+    std::vector<int32_t> big;
+    int64_t nsmall = 0;
+    int32_t last_v = -1;
+    bool bad = false;       // offsets decrease somewhere
+    double hist[kDegBins] = {};
+};
+
+void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
+{
+    int pv = 0, pe = 0;  // vertices / edges in the open pack
+    int64_t pstart = -1;
+    auto close = [&]() {
+        if (pv) {
+            P.pack_v0.push_back((int32_t)pstart);
+            P.pack_nv.push_back((uint8_t)pv);
+        }
+        pv = pe = 0;
+    };
+    for (int64_t v = v0; v < v1; ++v) {
+        const int64_t deg = off[v + 1] - off[v];
+        if (deg < 0) {
+            P.bad = true;
+            return;
+        }
+        if (deg > 0) {
+            P.last_v = (int32_t)v;
+            P.hist[std::min(kDegBins - 1, 63 - __builtin_clzll((unsigned long long)deg))] += (double)deg;
+        }
+        if (deg <= kSmallMax) {
+            if (pv == 32 || pe + deg > 32) close();
+            if (!pv) pstart = v;
+            pv++;
+            pe += (int)deg;
+            P.nsmall++;
+            continue;
+        }
+        close();
+        if (deg <= kXlMax) P.mid.push_back((int32_t)v);
+        else P.big.push_back((int32_t)v);
+    }
+    close();
+}
+
+}  // namespace
+
+// Static per-graph schedule (host), per scope: packs of consecutive vertices of degree
+// <= 32 (at most 32 vertices and 32 edges; a pack ends at a vertex of another bucket or
+// at a thread's chunk boundary), the mid list (33..12288) in ascending degree, and big
+// vertices (> 12288) with global hash tables (offsets relative to the scope, so
+// out-of-core batches reuse one table area) and their work chunks.  Vertex ranges are
+// planned by several host threads.  Returns false when the offsets decrease.
+bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts)
 {
     S = Schedule();
-    std::vector<int32_t> large, xl;
+    const int hw = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     for (size_t k = 0; k + 1 < scope_starts.size(); ++k) {
         Scope sc;
         sc.v0 = scope_starts[k];
@@ -71,73 +125,69 @@ void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         sc.b0 = (int32_t)S.big_v.size();
         sc.c0 = (int32_t)S.chunk_big.size();
         sc.s0 = (int32_t)S.schunk_big.size();
-        large.clear();
-        xl.clear();
-        int pv = 0, pe = 0;  // vertices / edges in the open pack
-        int64_t pstart = -1;
-        auto close = [&]() {
-            if (pv) {
-                S.pack_v0.push_back((int32_t)pstart);
-                S.pack_nv.push_back((uint8_t)pv);
+        const int64_t nv = sc.v1 - sc.v0;
+        const int T = nv >= (1 << 20) ? hw : 1;
+        std::vector<ChunkPlan> plans(T);
+        {
+            std::vector<std::thread> th;
+            for (int t = 0; t < T; ++t) {
+                const int64_t a = sc.v0 + nv * t / T, b = sc.v0 + nv * (t + 1) / T;
+                if (T == 1) plan_chunk(off, a, b, plans[t]);
+                else th.emplace_back(plan_chunk, off, a, b, std::ref(plans[t]));
             }
-            pv = pe = 0;
-            pstart = -1;
-        };
-        int64_t toff = 0, ooff = 0, nsmall = 0;
-        for (int64_t v = sc.v0; v < sc.v1; ++v) {
-            const int64_t deg = off[v + 1] - off[v];
-            if (deg > 0) sc.last_v = (int32_t)v;
-            if (deg <= kSmallMax) {
-                if (pv == 32 || pe + deg > 32) close();
-                if (!pv) pstart = v;
-                pv++;
-                pe += (int)deg;
-                nsmall++;
-                continue;
-            }
-            close();
-            if (deg <= kMidSMax) {
-                S.mid_v.push_back((int32_t)v);
-            } else if (deg <= kLargeMax) {
-                large.push_back((int32_t)v);
-            } else if (deg <= kXlMax) {
-                xl.push_back((int32_t)v);
-            } else {  // big: global table
-                const int32_t b = (int32_t)S.big_v.size();
-                S.big_v.push_back((int32_t)v);
-                uint32_t cap = 1;
-                while ((int64_t)cap < 2 * deg) cap <<= 1;
-                S.big_toff.push_back(toff);
-                S.big_tcap.push_back(cap);
-                S.big_ooff.push_back(ooff);
-                for (int64_t e = off[v]; e < off[v + 1]; e += kBigChunk) {
-                    S.chunk_big.push_back(b);
-                    S.chunk_e0.push_back(e);
-                    S.chunk_e1.push_back(std::min<int64_t>(e + kBigChunk, off[v + 1]));
-                }
-                for (int64_t i = 0; i < deg; i += kBigSlotChunk) {  // over the occupied list
-                    S.schunk_big.push_back(b);
-                    S.schunk_s0.push_back(i);
-                    S.schunk_s1.push_back(std::min<int64_t>(i + kBigSlotChunk, deg));
-                }
-                toff += cap;
-                ooff += deg;
-                S.m_big += deg;
-            }
+            for (auto &x : th) x.join();
         }
-        close();
-        sc.nms = (int32_t)S.mid_v.size() - sc.m0;
-        S.mid_v.insert(S.mid_v.end(), large.begin(), large.end());
-        sc.nml = (int32_t)large.size();
-        S.mid_v.insert(S.mid_v.end(), xl.begin(), xl.end());
-        sc.nmx = (int32_t)xl.size();
-        // the scope's mid list in ascending degree (stable): any degree threshold is a
-        // cut position, so the kernel split can change per iteration
-        std::stable_sort(S.mid_v.begin() + sc.m0, S.mid_v.end(), [off](int32_t x, int32_t y) {
-            return off[x + 1] - off[x] < off[y + 1] - off[y];
-        });
-        for (size_t i = (size_t)sc.m0; i < S.mid_v.size(); ++i)
-            S.mid_deg.push_back((int32_t)(off[S.mid_v[i] + 1] - off[S.mid_v[i]]));
+        int64_t nsmall = 0;
+        std::vector<int32_t> mid, big;
+        for (ChunkPlan &P : plans) {
+            if (P.bad) return false;
+            S.pack_v0.insert(S.pack_v0.end(), P.pack_v0.begin(), P.pack_v0.end());
+            S.pack_nv.insert(S.pack_nv.end(), P.pack_nv.begin(), P.pack_nv.end());
+            mid.insert(mid.end(), P.mid.begin(), P.mid.end());
+            big.insert(big.end(), P.big.begin(), P.big.end());
+            nsmall += P.nsmall;
+            if (P.last_v >= 0) sc.last_v = P.last_v;
+            for (int b = 0; b < kDegBins; ++b) S.deg_hist[b] += P.hist[b];
+        }
+        // the mid list in ascending degree (counting sort, stable): any degree threshold
+        // is a cut position, so the kernel split can change per iteration
+        {
+            std::vector<int64_t> at(kXlMax + 2, 0);
+            for (int32_t x : mid) ++at[(size_t)(off[x + 1] - off[x]) + 1];
+            for (size_t d = 1; d < at.size(); ++d) at[d] += at[d - 1];
+            sc.nms = (int32_t)at[kMidSMax + 1];
+            sc.nml = (int32_t)(at[kLargeMax + 1] - at[kMidSMax + 1]);
+            sc.nmx = (int32_t)(at[kXlMax + 1] - at[kLargeMax + 1]);
+            const size_t b = S.mid_v.size();
+            S.mid_v.resize(b + mid.size());
+            for (int32_t x : mid) S.mid_v[b + (size_t)at[(size_t)(off[x + 1] - off[x])]++] = x;
+            S.mid_deg.resize(S.mid_v.size());
+            for (size_t i = b; i < S.mid_v.size(); ++i) S.mid_deg[i] = (int32_t)(off[S.mid_v[i] + 1] - off[S.mid_v[i]]);
+        }
+        int64_t toff = 0, ooff = 0;
+        for (int32_t v : big) {
+            const int64_t deg = off[v + 1] - off[v];
+            const int32_t b = (int32_t)S.big_v.size();
+            S.big_v.push_back(v);
+            uint32_t cap = 1;
+            while ((int64_t)cap < 2 * deg) cap <<= 1;
+            S.big_toff.push_back(toff);
+            S.big_tcap.push_back(cap);
+            S.big_ooff.push_back(ooff);
+            for (int64_t e = off[v]; e < off[v + 1]; e += kBigChunk) {
+                S.chunk_big.push_back(b);
+                S.chunk_e0.push_back(e);
+                S.chunk_e1.push_back(std::min<int64_t>(e + kBigChunk, off[v + 1]));
+            }
+            for (int64_t i = 0; i < deg; i += kBigSlotChunk) {  // over the occupied list
+                S.schunk_big.push_back(b);
+                S.schunk_s0.push_back(i);
+                S.schunk_s1.push_back(std::min<int64_t>(i + kBigSlotChunk, deg));
+            }
+            toff += cap;
+            ooff += deg;
+            S.m_big += deg;
+        }
         sc.np = (int32_t)S.pack_v0.size() - sc.p0;
         sc.nb = (int32_t)S.big_v.size() - sc.b0;
         sc.nc = (int32_t)S.chunk_big.size() - sc.c0;
@@ -152,6 +202,7 @@ void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         S.max_scope_vertices = std::max(S.max_scope_vertices, sc.v1 - sc.v0);
         S.scopes.push_back(sc);
     }
+    return true;
 }
 
 int batch_boundaries(int64_t n, const int64_t *off, int buffer_pow, std::vector<int64_t> &bbs)
@@ -200,14 +251,23 @@ Engine::~Engine()
 
 int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_t &h2d)
 {
+    double tp = now_s();
+    auto phase = [&](int i) {
+        const double t = now_s();
+        setup_ms[i] += (t - tp) * 1e3;
+        tp = t;
+    };
     n = g.n;
     m = g.m;
     policy = o.policy;
+    {
+        int dev = 0;
+        GALP_CUDA(cudaGetDevice(&dev));
+        GALP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    }
     h_nbr = g.neighbors;
     frontier = o.frontier != 0 && policy == 0;  // the frontier needs the whole graph resident
     max_label = n;
-    for (int64_t v = 0; v < n; ++v)
-        if (g.offsets[v + 1] < g.offsets[v]) return GALP_EFORMAT;
     std::vector<int64_t> starts;
     if (policy == 0) {
         starts = {0, n};
@@ -216,7 +276,8 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
         int rc = batch_boundaries(n, g.offsets, o.buffer_pow, starts);
         if (rc) return rc;
     }
-    build_schedule(sched, n, g.offsets, starts);
+    if (!build_schedule(sched, n, g.offsets, starts)) return GALP_EFORMAT;
+    phase(0);
 
     GALP_CUDA(b_off.alloc(sizeof(int64_t) * (n + 1)));
     GALP_CUDA(cudaMemcpyAsync(b_off.p, g.offsets, sizeof(int64_t) * (n + 1), cudaMemcpyDefault, st));
@@ -242,6 +303,8 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
             GALP_CUDA(cudaEventCreateWithFlags(&ev_consumed[i], cudaEventDisableTiming));
         }
     }
+    GALP_CUDA(cudaStreamSynchronize(st));
+    phase(1);
     int rc;
     if ((rc = upload(b_pack_v0, d_pack_v0, sched.pack_v0, st, h2d))) return rc;
     if ((rc = upload(b_pack_nv, d_pack_nv, sched.pack_nv, st, h2d))) return rc;
@@ -270,17 +333,12 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     GALP_CUDA(b_tsmall.alloc(sizeof(int32_t) * (size_t)std::max<int64_t>(sched.max_scope_small, 1)));
     GALP_CUDA(b_tmid.alloc(sizeof(int32_t) * (size_t)std::max<int64_t>(sched.max_scope_mid, 1)));
     GALP_CUDA(b_bsum.alloc(sizeof(int64_t) * (size_t)std::max<int64_t>((sched.max_scope_vertices + kScanBlock - 1) / kScanBlock, 1)));
+    GALP_CUDA(cudaStreamSynchronize(st));
+    phase(2);
     // dispatch: static features, variant table, per-scope state, logs
     {
         float sf[kDegBins + 3] = {};
-        for (int64_t v = 0; v < n; ++v) {
-            const int64_t d = g.offsets[v + 1] - g.offsets[v];
-            if (d <= 0) continue;
-            int b = 0;
-            while (b < kDegBins - 1 && (d >> (b + 1))) ++b;
-            sf[b] += (float)d;
-        }
-        for (int b = 0; b < kDegBins; ++b) sf[b] = m > 0 ? sf[b] / (float)m : 0.f;
+        for (int b = 0; b < kDegBins; ++b) sf[b] = m > 0 ? (float)(sched.deg_hist[b] / (double)m) : 0.f;
         sf[kDegBins] = (float)(std::log2((double)std::max<int64_t>(m, 1)) / 40.0);
         sf[kDegBins + 1] = (float)(std::log2((double)std::max<int64_t>(n, 1)) / 40.0);
         sf[kDegBins + 2] = (float)(std::log2(std::max(1.0, (double)m / (double)std::max<int64_t>(n, 1))) / 16.0);
@@ -314,28 +372,29 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
         init_bigstat_kernel<<<(unsigned)((nbig + 255) / 256), 256, 0, st>>>((BigStat *)b_bstat.p, (int)nbig);
         GALP_CUDA(cudaGetLastError());
     }
+    phase(3);
     if (policy == 0) {
-        // validate the resident graph before any iteration touches it
+        // validate the resident graph before any iteration touches it; strictly increasing
+        // adjacency enables the first-iteration shortcut, a symmetric edge multiset the
+        // frontier (checked only when the frontier is wanted)
         GALP_CUDA(b_bad.alloc(sizeof(int)));
-        GALP_CUDA(cudaMemsetAsync(b_bad.p, 0, sizeof(int), st));
-        validate_kernel<<<1024, 256, 0, st>>>((const int32_t *)b_nbr[0].p, m, n, (int *)b_bad.p);
+        GALP_CUDA(b_chk.alloc(5 * sizeof(unsigned long long)));
+        GALP_CUDA(cudaMemsetAsync(b_chk.p, 0, 5 * sizeof(unsigned long long), st));
+        unsigned long long *dchk = (unsigned long long *)b_chk.p;
+        if (frontier) {  // rows needed for the checksum: one pass that knows each entry's row
+            adjacency_check_kernel<<<sms * 8, kTB, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p,
+                                                            n, 1, dchk);
+        } else {
+            csr_scan_kernel<<<sms * 16, kTB, 0, st>>>((const int32_t *)b_nbr[0].p, m, n, dchk);
+            row_start_kernel<<<sms * 8, kTB, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p, n, dchk);
+        }
         GALP_CUDA(cudaGetLastError());
-        int bad = 0;
-        GALP_CUDA(cudaMemcpyAsync(&bad, b_bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        GALP_CUDA(cudaStreamSynchronize(st));
-        if (bad) return GALP_EFORMAT;
-        // strictly increasing adjacency enables the first-iteration shortcut, a symmetric
-        // edge multiset the frontier
-        GALP_CUDA(b_chk.alloc(3 * sizeof(unsigned long long)));
-        GALP_CUDA(cudaMemsetAsync(b_chk.p, 0, 3 * sizeof(unsigned long long), st));
-        adjacency_check_kernel<<<1024, kTB, 0, st>>>((const int64_t *)b_off.p, (const int32_t *)b_nbr[0].p, n,
-                                                     (unsigned long long *)b_chk.p);
-        GALP_CUDA(cudaGetLastError());
-        unsigned long long chk[3] = {1, 1, 1};
+        unsigned long long chk[5] = {1, 1, 1, 1, 0};
         GALP_CUDA(cudaMemcpyAsync(chk, b_chk.p, sizeof(chk), cudaMemcpyDeviceToHost, st));
         GALP_CUDA(cudaStreamSynchronize(st));
-        adj_sorted = chk[0] == 0;
-        symmetric = chk[1] == 0 && chk[2] == 0;
+        if (chk[3]) return GALP_EFORMAT;
+        adj_sorted = chk[0] == chk[4];
+        symmetric = frontier && chk[1] == 0 && chk[2] == 0;
         if (!symmetric) frontier = false;
     }
     if (frontier) {
@@ -344,9 +403,9 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     }
     GALP_CUDA(cudaStreamSynchronize(st));
 
-    int dev = 0;
-    GALP_CUDA(cudaGetDevice(&dev));
-    GALP_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    phase(4);
+    GALP_CUDA(cudaFuncSetAttribute(count_cta_kernel<512, 2 * kXlAMax>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(unsigned long long) * 2 * kXlAMax)));
     GALP_CUDA(cudaFuncSetAttribute(count_cta_kernel<kXlThreads, kXlSlots>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)(sizeof(unsigned long long) * kXlSlots)));
@@ -455,6 +514,8 @@ void Engine::build_variant_table()
         d.agg_mode = (k & 8) ? 1 : 2;
         d.pos1 = cut((k & 4) ? 128 : kMidSMax);
         d.pos2 = cut((k & 2) ? 1024 : kLargeMax);
+        d.pos_a = std::max(d.pos1, cut(kLargeAMax));
+        d.pos_b = std::max(d.pos2, cut(kXlAMax));
         d.frontier = k & 1;
         d.variant = k;
     }
@@ -469,6 +530,10 @@ std::vector<DispatchState> Engine::static_dispatch() const
         ds[j].agg_mode = variant.agg_mode;
         ds[j].pos1 = sc.nms;
         ds[j].pos2 = sc.nms + sc.nml;
+        const int32_t *b = sched.mid_deg.data() + sc.m0;
+        const int cnt = sc.nms + sc.nml + sc.nmx;
+        ds[j].pos_a = (int32_t)(std::upper_bound(b, b + cnt, kLargeAMax) - b);
+        ds[j].pos_b = (int32_t)(std::upper_bound(b, b + cnt, kXlAMax) - b);
     }
     return ds;
 }
@@ -555,15 +620,25 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         count_mid_kernel<<<(int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1, (int64_t)sms * mid_bps),
                            32 * kMidWarps, 0, st>>>(q);
         launched("count_mid_kernel", st);
+        count_cta_kernel<128, 2 * kLargeAMax>
+            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 12)), 128,
+               sizeof(unsigned long long) * 2 * kLargeAMax, st>>>(q, 0);
+        launched("count_cta_kernel<128>", st);
         count_cta_kernel<kTB, 2 * kLargeMax>
-            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 6)), kTB,
-               sizeof(unsigned long long) * 2 * kLargeMax, st>>>(q, 0);
-        launched("count_cta_kernel<large>", st);
+            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * 6)), kTB,
+               sizeof(unsigned long long) * 2 * kLargeMax, st>>>(q, 1);
+        launched("count_cta_kernel<256>", st);
+        if (q.nmid_x + q.nmid_l) {
+            count_cta_kernel<512, 2 * kXlAMax>
+                <<<(int)std::max<int64_t>(1, std::min<int64_t>(q.nmid_x + q.nmid_l, (int64_t)sms * 2)), 512,
+                   sizeof(unsigned long long) * 2 * kXlAMax, st>>>(q, 2);
+            launched("count_cta_kernel<512>", st);
+        }
         if (q.nmid_x) {
             count_cta_kernel<kXlThreads, kXlSlots>
                 <<<(int)std::min<int64_t>(q.nmid_x, (int64_t)sms), kXlThreads, sizeof(unsigned long long) * kXlSlots,
-                   st>>>(q, 1);
-            launched("count_cta_kernel<xl>", st);
+                   st>>>(q, 3);
+            launched("count_cta_kernel<1024>", st);
         }
     }
     const int64_t nv = sc.v1 - sc.v0;
@@ -1027,6 +1102,7 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
     info->flags = (E.adj_sorted ? GALP_SCHED_SORTED : 0) | (E.symmetric ? GALP_SCHED_SYMMETRIC : 0) |
                   (E.frontier ? GALP_SCHED_FRONTIER : 0);
     info->launches = E.launches;
+    for (int i = 0; i < 5; ++i) info->setup_ms[i] = E.setup_ms[i];
     return GALP_OK;
 }
 

@@ -75,10 +75,12 @@ struct Schedule {
     std::vector<Scope> scopes;
     int64_t max_table_slots = 0, max_occ_slots = 0, max_scope_edges = 0, m_big = 0;
     int64_t max_scope_small = 0, max_scope_mid = 0, max_scope_vertices = 0;
+    double deg_hist[kDegBins] = {};  // CSR entries by log2 degree (dispatch features)
 };
 
-// Build the schedule; scope_starts = first vertex of every scope, then n.
-void build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts);
+// Build the schedule; scope_starts = first vertex of every scope, then n.  False when
+// the offsets decrease somewhere.
+bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts);
 
 // Batch boundaries of OutOfCore::compute_batch_boundaries (outofcore.cuh:38-60) for
 // 2^buffer_pow edges; returns GALP_EBATCH where the reference would loop forever.
@@ -204,6 +206,7 @@ struct Engine {
     uint64_t batch_seq = 0;   // running batch counter (buffer parity)
     int64_t h2d_run = 0;      // bytes streamed by the last run
     int64_t launches = 0;     // kernels launched by runs so far (setup excluded)
+    double setup_ms[5] = {};  // host schedule, CSR upload, state upload, dispatch prep, device checks
     // batched mode: graph g = vertices [g_v0[g], g_v0[g+1]) of the concatenated CSR
     bool batched = false;
     int32_t G = 0;

@@ -33,10 +33,12 @@ constexpr int kMaxLogIters = 64;
 struct DispatchState {
     int32_t agg_mode;  // CTA-table inserts: 0 auto, 1 warp-aggregated, 2 plain
     int32_t frontier;  // 1 = skip clean vertices this iteration (frontier mode only)
-    int32_t pos1;      // mid list [0, pos1): one warp each; [pos1, pos2): 256-thread CTA;
-    int32_t pos2;      // [pos2, end): 1024-thread CTA
+    // cuts of the degree-sorted mid list: [0, pos1) one warp each; [pos1, pos_a) 128-thread
+    // CTAs (degree <= 1024); [pos_a, pos2) 256-thread CTAs; [pos2, pos_b) 512-thread CTAs
+    // (degree <= 6144); [pos_b, end) 1024-thread CTAs
+    int32_t pos1, pos2, pos_a, pos_b;
     int32_t variant;   // row of the variant table
-    int32_t pad[3];
+    int32_t pad;
 };
 
 struct DispatchArgs {

@@ -37,9 +37,11 @@ constexpr int kMidSCap = 2 * kMidSMax;
 constexpr int kMidWarps = 8;         // warps (vertices) per mid CTA
 constexpr int kScanBlock = 4096;     // vertices per scan block (256 threads x 16)
 constexpr int kLargeMax = 2048;      // large bucket: 257..2048, one 256-thread CTA each
-constexpr int kXlMax = 12288;        // xl bucket: 2049..12288, one 1024-thread CTA each
+constexpr int kXlMax = 12288;        // xl bucket: 2049..12288, one CTA each (512 or 1024 threads)
 constexpr int kXlSlots = 2 * kXlMax; // 192 KB of shared-memory table (64-bit slots)
 constexpr int kXlThreads = 1024;
+constexpr int kLargeAMax = 1024;     // large vertices up to here: 128-thread CTAs, 16 KB tables
+constexpr int kXlAMax = 6144;        // xl vertices up to here: 512-thread CTAs, 96 KB tables
 
 struct PipeArgs {
     const int32_t *nbr;     // neighbour buffer holding CSR entries [nbr_shift, ...)
@@ -626,9 +628,13 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
 }
 
 // Block-wide Sum5 / pair reductions through shared memory (two barriers each).
+// Block-wide reductions with one barrier each: warps publish partials, then every warp
+// folds all of them.  Sum5 and the rank pair use separate buffers, and the kernel's
+// end-of-vertex barrier orders a buffer's reads before its next writes.
 template <int THREADS>
 struct BlockRed5 {
-    int (*buf)[32];  // [5][32]
+    int (*buf)[32];   // [5][32]
+    int (*buf2)[32];  // [2][32]
     __device__ Sum5 reduce(Sum5 s) const
     {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -641,58 +647,45 @@ struct BlockRed5 {
             buf[4][warp] = s.mx;
         }
         __syncthreads();
-        if (warp == 0) {
-            Sum5 t = sum5_empty();
-            if (lane < THREADS / 32) t = Sum5{buf[0][lane], buf[1][lane], buf[2][lane], buf[3][lane], buf[4][lane]};
-            t = sum5_warp(t);
-            if (lane == 0) {
-                buf[0][0] = t.d;
-                buf[1][0] = t.W;
-                buf[2][0] = t.k;
-                buf[3][0] = t.mn;
-                buf[4][0] = t.mx;
-            }
-        }
-        __syncthreads();
-        const Sum5 r{buf[0][0], buf[1][0], buf[2][0], buf[3][0], buf[4][0]};
-        return r;
+        Sum5 t = sum5_empty();
+        if (lane < THREADS / 32) t = Sum5{buf[0][lane], buf[1][lane], buf[2][lane], buf[3][lane], buf[4][lane]};
+        return sum5_warp(t);
     }
     __device__ void reduce2(int &a, int &b) const
     {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         a = __reduce_add_sync(kFull, a);
         b = __reduce_add_sync(kFull, b);
-        __syncthreads();  // buf may still be read from the previous reduction
         if (lane == 0) {
-            buf[0][warp] = a;
-            buf[1][warp] = b;
+            buf2[0][warp] = a;
+            buf2[1][warp] = b;
         }
         __syncthreads();
-        int x = 0, y = 0;
-        for (int i = 0; i < THREADS / 32; ++i) {
-            x += buf[0][i];
-            y += buf[1][i];
-        }
-        a = x;
-        b = y;
+        const int x = lane < THREADS / 32 ? buf2[0][lane] : 0, y = lane < THREADS / 32 ? buf2[1][lane] : 0;
+        a = __reduce_add_sync(kFull, x);
+        b = __reduce_add_sync(kFull, y);
     }
 };
 
 // One CTA of THREADS threads per vertex of degree <= SLOTS/2 (table of SLOTS 64-bit
 // slots in dynamic shared memory), for a range of the degree-sorted mid list.
 template <int THREADS, int SLOTS>
-__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : 6) count_cta_kernel(PipeArgs p, int which)
+__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 ? 2 : THREADS >= 256 ? 6 : 12)
+    count_cta_kernel(PipeArgs p, int which)
 {
     extern __shared__ __align__(16) unsigned long long cta_tab[];
-    __shared__ int red[5][32];
+    __shared__ int red[5][32], red2[2][32];
     __shared__ int sctr;
     if (!ctl_active(p.ctl)) return;
-    // which 0: mid list [pos1, pos2); which 1: [pos2, end)
-    const int first = which == 0 ? p.disp->pos1 : p.disp->pos2;
-    const int count = (which == 0 ? p.disp->pos2 : p.nmid_s + p.nmid_l + p.nmid_x) - first;
+    // ranges of the degree-sorted mid list: 0 [pos1, pos_a), 1 [pos_a, pos2), 2 [pos2, pos_b),
+    // 3 [pos_b, end)
+    const DispatchState &ds = *p.disp;
+    const int first = which == 0 ? ds.pos1 : which == 1 ? ds.pos_a : which == 2 ? ds.pos2 : ds.pos_b;
+    const int end = which == 0 ? ds.pos_a : which == 1 ? ds.pos2 : which == 2 ? ds.pos_b : p.nmid_s + p.nmid_l + p.nmid_x;
+    const int count = end - first;
     const bool fr = frontier_on(p);
     const int tid = threadIdx.x;
-    const BlockRed5<THREADS> br{red};
+    const BlockRed5<THREADS> br{red, red2};
     unsigned long long changes = 0;
     for (int s = tid; s < SLOTS; s += THREADS) cta_tab[s] = 0ull;
     uint32_t gen = 0;
@@ -1122,26 +1115,62 @@ __global__ void __launch_bounds__(kTB) first_iteration_kernel(PipeArgs p, int64_
     flush_changes(changes, p.ctl);
 }
 
+// Setup checks without the symmetry checksum, as two streaming passes:
+//   csr_scan_kernel:     out[3] += neighbour IDs outside [0, n); out[0] += entries e >= 1
+//                        with nbr[e] <= nbr[e-1] (all descents, row boundaries included);
+//   row_start_kernel:    out[4] += those descents that sit at a row start (e = offsets[v]
+//                        of a vertex with neighbours), which do not count.
+// Adjacency lists are strictly increasing when out[0] == out[4].
+__global__ void __launch_bounds__(kTB) csr_scan_kernel(const int32_t *nbr, int64_t m, int64_t n,
+                                                       unsigned long long *out)
+{
+    unsigned long long desc = 0, outside = 0;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t u = __ldg(&nbr[e]);
+        outside += (u < 0 || u >= n);
+        if (e > 0) desc += (u <= __ldg(&nbr[e - 1]));
+    }
+    desc = __reduce_add_sync(kFull, (unsigned)desc);
+    outside = __reduce_add_sync(kFull, (unsigned)outside);
+    if ((threadIdx.x & 31) == 0) {
+        if (desc) atomicAdd(&out[0], desc);
+        if (outside) atomicAdd(&out[3], outside);
+    }
+}
+
+__global__ void __launch_bounds__(kTB) row_start_kernel(const int64_t *off, const int32_t *nbr, int64_t n,
+                                                        unsigned long long *out)
+{
+    unsigned long long b = 0;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = off[v];
+        if (e > 0 && off[v + 1] > e) b += (__ldg(&nbr[e]) <= __ldg(&nbr[e - 1]));
+    }
+    b = __reduce_add_sync(kFull, (unsigned)b);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(&out[4], b);
+}
+
 // One pass over the resident CSR at setup (warp per 32 consecutive vertices, lanes over
 // the warp's edge range, row of each edge by a shuffle binary search over the 33 offsets):
+//   out[3] += neighbour IDs outside [0, n) (the graph is rejected);
 //   out[0] += adjacent entries of one row that are not strictly increasing
 //             (0 enables the first-iteration shortcut);
 //   out[1], out[2] += sum over entries (v, u) of g(v)k(u) - g(u)k(v) (mod 2^64) for two
 //             hash pairs g, k.  The form is antisymmetric, so every graph whose edge
 //             multiset is symmetric sums to 0 in both; an asymmetric one does so only by a
 //             hash collision (about 2^-64 per sum).  Both 0 enables the frontier, whose
-//             dirty marking pushes along out-edges.
+//             dirty marking pushes along out-edges.  Computed only when want_sym.
 __device__ __forceinline__ uint64_t adj_hash(uint64_t x, uint64_t salt)
 {
     return splitmix64_mix(x * 0x9E3779B97F4A7C15ull + salt);
 }
 
 __global__ void __launch_bounds__(kTB) adjacency_check_kernel(const int64_t *off, const int32_t *nbr, int64_t n,
-                                                              unsigned long long *out)
+                                                              int want_sym, unsigned long long *out)
 {
     const int lane = threadIdx.x & 31;
     const int64_t nwb = (n + 31) >> 5;
-    unsigned long long desc = 0, s1 = 0, s2 = 0;
+    unsigned long long desc = 0, s1 = 0, s2 = 0, outside = 0;
     for (int64_t wb = (int64_t)(blockIdx.x * blockDim.x + threadIdx.x) >> 5; wb < nwb;
          wb += (int64_t)(gridDim.x * blockDim.x) >> 5) {
         const int64_t vb = wb << 5;
@@ -1165,6 +1194,9 @@ __global__ void __launch_bounds__(kTB) adjacency_check_kernel(const int64_t *off
             const int64_t row_start = __shfl_sync(kFull, o, r);
             if (valid) {
                 if (e != row_start && u <= prev) ++desc;
+                outside += (u < 0 || u >= n);
+            }
+            if (valid && want_sym) {
                 const uint64_t v = (uint64_t)(vb + r);
                 s1 += adj_hash(v, 0x1234567ull) * adj_hash((uint64_t)u, 0xABCDEF1ull) -
                       adj_hash((uint64_t)u, 0x1234567ull) * adj_hash(v, 0xABCDEF1ull);
@@ -1178,11 +1210,15 @@ __global__ void __launch_bounds__(kTB) adjacency_check_kernel(const int64_t *off
         desc += __shfl_xor_sync(kFull, desc, sh);
         s1 += __shfl_xor_sync(kFull, s1, sh);
         s2 += __shfl_xor_sync(kFull, s2, sh);
+        outside += __shfl_xor_sync(kFull, outside, sh);
     }
     if (lane == 0) {
         if (desc) atomicAdd(&out[0], desc);
-        atomicAdd(&out[1], s1);
-        atomicAdd(&out[2], s2);
+        if (want_sym) {
+            atomicAdd(&out[1], s1);
+            atomicAdd(&out[2], s2);
+        }
+        if (outside) atomicAdd(&out[3], outside);
     }
 }
 

@@ -10,7 +10,7 @@ class SchedInfo(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("m", ctypes.c_int64), ("m_big", ctypes.c_int64), ("npacks", ctypes.c_int64),
                 ("nmid", ctypes.c_int64), ("nlarge", ctypes.c_int64), ("nbig", ctypes.c_int64),
                 ("table_slots", ctypes.c_int64), ("launches_per_iter", ctypes.c_int32), ("flags", ctypes.c_int32),
-                ("launches", ctypes.c_int64)]
+                ("launches", ctypes.c_int64), ("setup_ms", ctypes.c_double * 5)]
 
     SORTED = 1
     SYMMETRIC = 2

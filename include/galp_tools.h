@@ -26,6 +26,8 @@ typedef struct {
     int32_t launches_per_iter; /* kernels launched per dense iteration (upper bound) */
     int32_t flags;         /* GALP_SCHED_* bits */
     int64_t launches;      /* kernels launched by the context's runs so far (setup excluded) */
+    double setup_ms[5];    /* galp_create phases: host schedule, CSR upload, schedule upload and
+                              per-vertex state, dispatch preparation, device checks */
 } galp_sched_info;
 
 #define GALP_SCHED_SORTED 1     /* every adjacency list strictly increasing */
