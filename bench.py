@@ -356,13 +356,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(workload: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+def ncu_traffic(workload: str, group: str):
+    """DRAM bytes per iteration of a kernel group from the committed ncu summary (None
+    when that workload was not captured)."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if os.path.exists(path):
         with open(path) as f:
             d = json.load(f)
-        return d.get(workload)
+        v = d.get(workload, {})
+        return v.get(group) if isinstance(v, dict) else None
     return None
 
 
@@ -427,7 +429,8 @@ def run_gpu(args, g, desc, rank, world, dist):
     # a dedicated stream: the library launches on it and the events are recorded on it
     stream = torch.cuda.Stream()
     # device-resident arm
-    p = galp_gb300.Propagator(g, early_exit=0, device=dev)
+    ooc = dict(policy=args.policy, buffer_pow=args.buffer_pow) if args.policy else {}
+    p = galp_gb300.Propagator(g, early_exit=0, device=dev, **ooc)
     p.set_stream(stream.cuda_stream)
     info = tools.schedule_info(p)
     for _ in range(args.warmup):
@@ -478,7 +481,7 @@ def run_gpu(args, g, desc, rank, world, dist):
         dur = (kt.big_pre_ms + kt.big_post_ms) / launches
         alg = big_bytes
     achieved = alg / (dur / 1e3) / 1e9
-    traffic = ncu_traffic(desc["workload"])
+    traffic = ncu_traffic(desc["workload"], dom)
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": int(alg), "avg_launch_ms": round(dur, 4),
@@ -488,7 +491,7 @@ def run_gpu(args, g, desc, rank, world, dist):
 
     # frontier mode under the fixed rule and the learned dispatcher (same labels)
     dispatch = None
-    if not args.no_dispatch:
+    if not args.no_dispatch and not args.policy:
         dispatch = {"frontier": True, "iterations": NITER}
         for name, kw in (("fixed", {}), ("learned", {"dispatch": 1})):
             try:
@@ -523,7 +526,7 @@ def run_gpu(args, g, desc, rank, world, dist):
             dist.barrier()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        q = galp_gb300.Propagator(g, early_exit=0, device=dev)
+        q = galp_gb300.Propagator(g, early_exit=0, device=dev, **ooc)
         q.run(NITER)
         lab = q.get_labels()
         h2d, d2h = q.stats.h2d_bytes, q.stats.d2h_bytes
@@ -546,11 +549,13 @@ def run_gpu(args, g, desc, rank, world, dist):
                "sample": (f"one sweep of CPUWorker::update_label (port) over vertices [0, {s['vertices']}) = "
                           f"{s['edges']} of {g.m} CSR entries, OpenMP dynamic schedule")}
     cfg = dict(desc)
-    cfg.update(iterations_per_step=NITER, early_exit=False, method=0, policy=0,
+    cfg.update(iterations_per_step=NITER, early_exit=False, method=0, policy=args.policy,
                l2="inputs larger than L2 (neighbours {:.1f} GB vs 129 MB L2)".format(4 * g.m / 1e9),
                parallelism="replicas" if world > 1 else "single-gpu", packs=int(info.npacks),
                mid_vertices=int(info.nmid), large_vertices=int(info.nlarge), big_vertices=int(info.nbig),
                big_edges=int(info.m_big))
+    if args.policy:
+        cfg["buffer_pow"] = args.buffer_pow
     line = {
         "metric": "GTEPS per LP iteration", "value": round(value, 3), "unit": "GTEPS", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
@@ -577,6 +582,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dispatch", action="store_true")
+    ap.add_argument("--policy", type=int, default=0, choices=[0, 1, 2],
+                    help="1/2: out-of-core, neighbours streamed from pinned host memory in 2^buffer_pow chunks")
+    ap.add_argument("--buffer-pow", type=int, default=24)
+    ap.add_argument("--case", type=int, default=0,
+                    help="profiler case: build the workload, run this many iterations once, print a summary")
     args = ap.parse_args()
     rank, world, local = _rank_env()
 
@@ -609,6 +619,15 @@ def main():
         build()
     if dist:
         dist.barrier()
+    if args.case:
+        import galp_gb300
+
+        g, desc = build_workload(args.workload)
+        with galp_gb300.Propagator(g, early_exit=0) as p:
+            p.run(args.case)
+            print(json.dumps({"case": desc["workload"], "n": desc["n"], "m": desc["m"], "iterations": p.iters_run,
+                              "updates": list(p.updates)[:p.iters_run]}))
+        return 0
     if WORKLOADS[args.workload][0] == "batch":
         line = run_batch(args, WORKLOADS[args.workload][1]["count"])
         if rank == 0:
