@@ -472,20 +472,22 @@ def run_gpu(args, g, desc, rank, world, dist):
     big_bytes = 8 * mb
     shares = {"count_scan_resolve": kt.pipe_ms, "big_vertex_kernels": kt.big_pre_ms + kt.big_post_ms}
     dom = max(shares, key=shares.get)
+    # per iteration: one group per scope (every out-of-core batch is its own scope)
+    iters = max(args.steps * NITER, 1)
     if dom == "count_scan_resolve":
-        launches = max(kt.pipe_groups, 1)
-        dur = kt.pipe_ms / launches
+        dur = kt.pipe_ms / iters
         alg = pipe_bytes
     else:
-        launches = max(kt.big_pre_groups, 1)
-        dur = (kt.big_pre_ms + kt.big_post_ms) / launches
+        dur = (kt.big_pre_ms + kt.big_post_ms) / iters
         alg = big_bytes
     achieved = alg / (dur / 1e3) / 1e9
-    traffic = ncu_traffic(desc["workload"], dom)
+    traffic = ncu_traffic(desc["workload"], dom) if not args.policy else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": int(alg), "avg_launch_ms": round(dur, 4),
                 "kernel_share": {k: round(v / max(sum(shares.values()), 1e-9), 3) for k, v in shares.items()}}
+    if args.policy:  # out-of-core: the neighbours cross the host link every iteration
+        roofline["h2d_GBps_per_iteration"] = round(4 * m / (ms_per_step / NITER / 1e3) / 1e9, 1)
     p.close()
     del p
 

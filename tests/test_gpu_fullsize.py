@@ -1,5 +1,7 @@
 """Parity at benchmark-like sizes.
 
+* LFR-style n = 1 M (the LFR configuration, methods 0 and 1): labels, iteration count and
+  change counts equal the oracle after 10 iterations.
 * R-MAT scale 22 (2.4 M vertices, 128 M CSR entries): labels and change counts equal the
   oracle after each of the first four iterations.
 * R-MAT scale 24 (8.9 M vertices, 521 M CSR entries, the R-MAT 24 configuration): the
@@ -82,3 +84,15 @@ def test_rmat24_properties_on_a_sample():
             new = p.get_labels()
             _check_step(g, prev, new, sample)
             prev = new
+
+
+def test_lfr_1m_ten_iterations_equal_the_oracle():
+    # the LFR-style configuration at full size: n = 1,000,000, mean degree 20
+    g = galp_gb300.generate_lfr(1_000_000, seed=1)
+    for method in (0, 1):
+        with galp_gb300.Propagator(g, method=method) as p:
+            p.run(10)
+            got, its, upd = p.get_labels(), p.iters_run, list(p.updates)
+        it, want, counts = oracle.run(g.offsets, g.neighbors, 10)
+        assert its == it and upd == list(counts)
+        assert np.array_equal(got, want)
