@@ -361,12 +361,21 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     const size_t nbig = sched.big_v.size();
     GALP_CUDA(b_bstat.alloc(sizeof(BigStat) * std::max<size_t>(nbig, 1)));
     GALP_CUDA(b_big_a.alloc(sizeof(int64_t) * std::max<size_t>(nbig, 1)));
-    GALP_CUDA(b_gkey.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.max_table_slots, 1)));
-    GALP_CUDA(b_gcnt.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.max_table_slots, 1)));
+    GALP_CUDA(b_gtab.alloc(sizeof(unsigned long long) * std::max<int64_t>(sched.max_table_slots, 1)));
     GALP_CUDA(b_occ.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.max_occ_slots, 1)));
     if (sched.max_table_slots) {
-        GALP_CUDA(cudaMemsetAsync(b_gkey.p, 0xFF, sizeof(uint32_t) * sched.max_table_slots, st));
-        GALP_CUDA(cudaMemsetAsync(b_gcnt.p, 0, sizeof(uint32_t) * sched.max_table_slots, st));
+        GALP_CUDA(cudaMemsetAsync(b_gtab.p, 0, sizeof(unsigned long long) * sched.max_table_slots, st));
+        // slot layout: generation | label | count, counts up to the largest hub degree
+        int64_t maxdeg = 1;
+        for (int32_t v : sched.big_v) maxdeg = std::max<int64_t>(maxdeg, g.offsets[v + 1] - g.offsets[v]);
+        int cb = 1, lb = 1;
+        while (cb < 31 && (maxdeg >> cb)) ++cb;
+        while (lb < 31 && ((std::max<int64_t>(n, 2) - 1) >> lb)) ++lb;
+        hub_cbits = cb;
+        hub_gshift = cb + lb;
+        hub_lmask = lb >= 32 ? 0xFFFFFFFFu : ((1u << lb) - 1u);
+        hub_gen_max = (uint32_t)std::min<int64_t>(((int64_t)1 << std::min(64 - cb - lb, 31)) - 1, 0x7FFFFFFF);
+        hub_gen = 0;
     }
     if (nbig) {
         init_bigstat_kernel<<<(unsigned)((nbig + 255) / 256), 256, 0, st>>>((BigStat *)b_bstat.p, (int)nbig);
@@ -487,8 +496,11 @@ IterArgs Engine::big_args(const Scope &sc) const
     a.schunk_s0 = d_schunk_s0;
     a.schunk_s1 = d_schunk_s1;
     a.nschunks = sc.ns;
-    a.gkey = (uint32_t *)b_gkey.p;
-    a.gcnt = (uint32_t *)b_gcnt.p;
+    a.gtab = (unsigned long long *)b_gtab.p;
+    a.hub_gen = hub_gen;
+    a.hub_cbits = hub_cbits;
+    a.hub_gshift = hub_gshift;
+    a.hub_lmask = hub_lmask;
     a.bstat = (BigStat *)b_bstat.p;
     a.big_a = (int64_t *)b_big_a.p;
     a.big_occ = (uint32_t *)b_occ.p;
@@ -582,6 +594,12 @@ PipeArgs Engine::pipe_args(const Scope &sc) const
 int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
                           int32_t *lab_out, const uint8_t *dirty, int32_t *changed)
 {
+    if (sc.nb) {  // a new generation for the hub tables: the previous scope's slots turn free
+        if (++hub_gen > hub_gen_max) {
+            GALP_CUDA(cudaMemsetAsync(b_gtab.p, 0, b_gtab.bytes, st));
+            hub_gen = 1;
+        }
+    }
     IterArgs a = big_args(sc);
     a.nbr = nbr;
     a.lab_in = lab_in;
@@ -667,8 +685,6 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         if (prof.on) e0 = prof.mark(st);
         big_resolve_kernel<<<a.nbig, 32, sizeof(uint32_t) * kPickScratch, st>>>(a);
         launched("big_resolve_kernel", st);
-        big_clear_kernel<<<a.nschunks, kTB, 0, st>>>(a);
-        launched("big_clear_kernel", st);
         big_reset_kernel<<<(a.nbig + 255) / 256, 256, 0, st>>>(a);
         launched("big_reset_kernel", st);
         if (prof.on) prof.spans[2].push_back({e0, prof.mark(st)});
@@ -1098,7 +1114,7 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
     info->nlarge = nml;
     info->nbig = (int64_t)E.sched.big_v.size();
     info->table_slots = E.sched.max_table_slots;
-    info->launches_per_iter = 10 + (info->nbig ? 8 : 0) + (E.frontier ? 1 : 0);
+    info->launches_per_iter = 14 + (info->nbig ? 7 : 0) + (E.frontier ? 1 : 0);
     info->flags = (E.adj_sorted ? GALP_SCHED_SORTED : 0) | (E.symmetric ? GALP_SCHED_SYMMETRIC : 0) |
                   (E.frontier ? GALP_SCHED_FRONTIER : 0);
     info->launches = E.launches;

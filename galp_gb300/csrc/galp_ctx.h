@@ -175,7 +175,7 @@ struct Engine {
     Schedule sched;
     DevBuf b_nbr[2], b_off, b_pack_v0, b_pack_nv, b_mid_v, b_big_v, b_big_toff, b_big_tcap;
     DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff;
-    DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_gkey, b_gcnt, b_occ, b_bad;
+    DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_gtab, b_occ, b_bad;
     DevBuf b_dcnt, b_runbase, b_c0, b_c1, b_kw, b_r, b_run_lab, b_run_cnt, b_tsmall, b_tmid, b_bsum;
     DevBuf b_dirty, b_changed, b_chk;  // frontier mode; setup adjacency checks
     DevBuf b_static_feat, b_vtab, b_disp, b_feat_log, b_var_log, b_weights;  // dispatch
@@ -206,6 +206,9 @@ struct Engine {
     uint64_t batch_seq = 0;   // running batch counter (buffer parity)
     int64_t h2d_run = 0;      // bytes streamed by the last run
     int64_t launches = 0;     // kernels launched by runs so far (setup excluded)
+    // hub tables: generation of the scope being enqueued, slot layout
+    uint32_t hub_gen = 0, hub_gen_max = 1, hub_lmask = 0;
+    int hub_cbits = 1, hub_gshift = 2;
     double setup_ms[5] = {};  // host schedule, CSR upload, state upload, dispatch prep, device checks
     // batched mode: graph g = vertices [g_v0[g], g_v0[g+1]) of the concatenated CSR
     bool batched = false;

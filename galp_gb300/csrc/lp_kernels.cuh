@@ -106,8 +106,11 @@ struct IterArgs {
     const int64_t *schunk_s0;   // stats chunk -> first entry of the vertex's occupied list
     const int64_t *schunk_s1;
     int32_t nschunks;
-    uint32_t *gkey;             // big tables: keys
-    uint32_t *gcnt;             // big tables: counts
+    unsigned long long *gtab;   // big tables: 64-bit slots generation | label | count
+    uint32_t hub_gen;           // generation of this scope's tables (slots of others are free)
+    int32_t hub_cbits;          // count bits (counts <= the largest hub degree)
+    int32_t hub_gshift;         // generation shift = count bits + label bits
+    uint32_t hub_lmask;         // label mask after the count shift
     BigStat *bstat;
     int64_t *big_a;             // run base of each big vertex (written by the scan)
     uint32_t *big_occ;          // occupied-slot list of each big table (capacity = degree)
@@ -332,11 +335,30 @@ struct RunListQuery {
     }
 };
 
-// Open-addressed table region (keys/counts) of one vertex, scanned by one warp.
-// hist: 256 ints of warp-private shared memory.
-struct WarpTableQuery {
+// Table layouts a WarpTableQueryT reads: k(s) = label of slot s or kEmpty, c(s) = its count.
+struct SplitTable {  // separate key and count arrays (shared-memory regions)
     const uint32_t *key;
     const uint32_t *cnt;
+    __device__ uint32_t k(int s) const { return key[s]; }
+    __device__ uint32_t c(int s) const { return cnt[s]; }
+};
+struct HubTable {  // generation-tagged 64-bit slots (global hub tables)
+    const unsigned long long *tab;
+    int cbits, gshift;
+    uint32_t lmask, gen;
+    __device__ uint32_t k(int s) const
+    {
+        const unsigned long long x = tab[s];
+        return (uint32_t)(x >> gshift) == gen ? (uint32_t)(x >> cbits) & lmask : kEmpty;
+    }
+    __device__ uint32_t c(int s) const { return (uint32_t)(tab[s] & ((1ull << cbits) - 1)); }
+};
+
+// Open-addressed table region of one vertex, scanned by one warp.
+// hist: 256 ints of warp-private shared memory.
+template <class T>
+struct WarpTableQueryT {
+    T t;
     int cap;
     int d, W, rmin, rmax;
     int *hist;
@@ -358,7 +380,7 @@ struct WarpTableQuery {
             __syncwarp();
             const uint32_t hi_mask = (shift == 24) ? 0u : (0xFFFFFFFFu << (shift + 8));
             for (int i = lane; i < nslots(); i += 32) {
-                uint32_t k = key[slot(i)];
+                uint32_t k = t.k(slot(i));
                 if (k != kEmpty && (k & hi_mask) == (prefix & hi_mask)) atomicAdd(&hist[(k >> shift) & 255], 1);
             }
             __syncwarp();
@@ -403,7 +425,7 @@ struct WarpTableQuery {
     {
         int n = 0;
         for (int i = lane; i < nslots(); i += 32) {
-            uint32_t k = key[slot(i)];
+            uint32_t k = t.k(slot(i));
             n += (k != kEmpty && k < c);
         }
         return __reduce_add_sync(kFull, n);
@@ -416,8 +438,8 @@ struct WarpTableQuery {
         uint32_t best = kEmpty;
         for (int i = lane; i < nslots(); i += 32) {
             const int s = slot(i);
-            uint32_t k = key[s];
-            if (k != kEmpty && (int)cnt[s] == W && k >= L && k < best) best = k;
+            uint32_t k = t.k(s);
+            if (k != kEmpty && (int)t.c(s) == W && k >= L && k < best) best = k;
         }
         best = __reduce_min_sync(kFull, best);
         if (best == kEmpty) return -1;
@@ -431,8 +453,8 @@ struct WarpTableQuery {
         int best = -1;
         for (int i = lane; i < nslots(); i += 32) {
             const int s = slot(i);
-            uint32_t k = key[s];
-            if (k != kEmpty && (int)cnt[s] == W && k < L && (int)k > best) best = (int)k;
+            uint32_t k = t.k(s);
+            if (k != kEmpty && (int)t.c(s) == W && k < L && (int)k > best) best = (int)k;
         }
         best = __reduce_max_sync(kFull, best);
         if (best < 0) return -1;
@@ -442,8 +464,8 @@ struct WarpTableQuery {
     {
         uint32_t h = hslot(k, (uint32_t)cap);
         for (int probes = 0; probes < cap; ++probes) {
-            const uint32_t x = key[h];
-            if (x == k) return cnt[h];
+            const uint32_t x = t.k((int)h);
+            if (x == k) return t.c((int)h);
             if (x == kEmpty) return 0;
             h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
         }
@@ -459,7 +481,7 @@ struct WarpTableQuery {
         int base = 0;
         for (int i0 = 0; i0 < nslots(); i0 += 32) {
             const int i = i0 + lane;
-            const uint32_t k = (i < nslots()) ? key[slot(i)] : kEmpty;
+            const uint32_t k = (i < nslots()) ? t.k(slot(i)) : kEmpty;
             const bool in = k != kEmpty && k >= Llo && k < Lhi;
             const unsigned m = __ballot_sync(kFull, in);
             if (in && base + __popc(m & ((1u << lane) - 1)) < kPickScratch)
@@ -498,6 +520,7 @@ struct WarpTableQuery {
         return (int)lo + __shfl_sync(kFull, bi, __ffs(m) - 1);
     }
 };
+using WarpTableQuery = WarpTableQueryT<SplitTable>;
 
 // ---------------------------------------------------------------------------
 // the tile kernel
@@ -887,7 +910,7 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
                 const int deg = vdeg(S, i);
                 const int d = S.vd[i], W = S.vW[i];
                 const long long a = S.P + S.vpref[i];
-                WarpTableQuery q{&S.hkey[2 * S.vpos[i]], &S.hcnt[2 * S.vpos[i]], 2 * pad32(deg), d, W,
+                WarpTableQuery q{{&S.hkey[2 * S.vpos[i]], &S.hcnt[2 * S.vpos[i]]}, 2 * pad32(deg), d, W,
                                  S.vrmin[i], S.vrmax[i], hist, lane, nullptr};
                 if (r < 0) r = resolve_rank(a, d, S.N, v == p.last_v, q);
                 const int32_t label =
@@ -914,7 +937,7 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
 
 // Count the labels of one chunk of a big vertex's edges in shared memory, then merge
 // the distinct (label, count) pairs into the vertex's global table.
-__global__ void __launch_bounds__(kTB) big_insert_kernel(IterArgs p)
+__global__ void __launch_bounds__(kTB, 3) big_insert_kernel(IterArgs p)
 {
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
@@ -957,34 +980,80 @@ __global__ void __launch_bounds__(kTB) big_insert_kernel(IterArgs p)
         }
     }
     __syncthreads();
+    // Merge into the vertex's global table of generation-tagged 64-bit slots: a slot of
+    // another generation is free, so tables are never cleared between iterations.  The
+    // count is the low field; a 32-bit add on the slot's low word never carries into the
+    // label (a count stays below 2^hub_cbits).
     const int64_t toff = p.big_toff[bi];
     const uint32_t gcap = p.big_tcap[bi];
-    uint32_t *gk = p.gkey + toff;
-    uint32_t *gc = p.gcnt + toff;
+    unsigned long long *gt = p.gtab + toff;
     uint32_t *occ = p.big_occ + p.big_ooff[bi];
     int *dcount = &p.bstat[bi].d;
     const int lane = threadIdx.x & 31;
-    constexpr int U = 8;  // slots per thread with their table CAS in flight together
+    const uint32_t gen = p.hub_gen;
+    constexpr int U = 4;  // slots per thread with their table reads in flight together
     for (int base = 0; base < (int)cap; base += kTB * U) {  // cap is a multiple of kTB * U
-        uint32_t L[U], h[U], prev[U];
+        uint32_t L[U], h[U];
+        unsigned long long cur[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             L[u] = skey[base + u * kTB + threadIdx.x];
             h[u] = (L[u] != kEmpty) ? hslot(L[u], gcap) : 0;
         }
 #pragma unroll
-        for (int u = 0; u < U; ++u) prev[u] = (L[u] != kEmpty) ? atomicCAS(&gk[h[u]], kEmpty, L[u]) : kEmpty;
+        for (int u = 0; u < U; ++u) cur[u] = (L[u] != kEmpty) ? *(volatile unsigned long long *)&gt[h[u]] : 0ull;
+        // first attempt for all U slots together: add to a slot holding the label, or
+        // claim a free one (the claims' compare-and-swaps in flight together)
+        unsigned long long tag[U], prev[U];
+        uint32_t c[U];
+        int state[U];  // 0 nothing to do, 1 done, 2 claim issued, 3 probe on
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            state[u] = 0;
+            if (L[u] == kEmpty) continue;
+            c[u] = scnt[base + u * kTB + threadIdx.x];
+            tag[u] = ((unsigned long long)gen << p.hub_gshift) | ((unsigned long long)L[u] << p.hub_cbits);
+            if ((cur[u] >> p.hub_cbits) == (tag[u] >> p.hub_cbits)) {  // same generation and label
+                atomicAdd((unsigned int *)&gt[h[u]], c[u]);
+                state[u] = 1;
+            } else {
+                state[u] = (uint32_t)(cur[u] >> p.hub_gshift) != gen ? 2 : 3;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (state[u] == 2) prev[u] = atomicCAS(&gt[h[u]], cur[u], tag[u] | c[u]);
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             bool created = false;
-            if (L[u] != kEmpty) {
-                // linear probing past slots owned by other labels (rare at load <= 1/2)
-                while (prev[u] != kEmpty && prev[u] != L[u]) {
-                    h[u] = (h[u] + 1 == gcap) ? 0 : h[u] + 1;
-                    prev[u] = atomicCAS(&gk[h[u]], kEmpty, L[u]);
+            if (state[u] == 2) {
+                if (prev[u] == cur[u]) {
+                    created = true;
+                    state[u] = 1;
+                } else {
+                    cur[u] = prev[u];
+                    state[u] = 3;
                 }
-                created = prev[u] == kEmpty;
-                atomicAdd(&gc[h[u]], scnt[base + u * kTB + threadIdx.x]);
+            }
+            if (state[u] == 3) {  // the slot changed or belongs to another label
+                for (;;) {
+                    if ((cur[u] >> p.hub_cbits) == (tag[u] >> p.hub_cbits)) {
+                        atomicAdd((unsigned int *)&gt[h[u]], c[u]);
+                        break;
+                    }
+                    if ((uint32_t)(cur[u] >> p.hub_gshift) != gen) {  // free: claim it
+                        const unsigned long long pv = atomicCAS(&gt[h[u]], cur[u], tag[u] | c[u]);
+                        if (pv == cur[u]) {
+                            created = true;
+                            break;
+                        }
+                        cur[u] = pv;
+                        continue;
+                    }
+                    // linear probing past slots owned by other labels (rare at load <= 1/2)
+                    h[u] = (h[u] + 1 == gcap) ? 0 : h[u] + 1;
+                    cur[u] = *(volatile unsigned long long *)&gt[h[u]];
+                }
             }
             // record newly occupied slots in the vertex's occupied list (warp-aggregated)
             const unsigned m = __ballot_sync(kFull, created);
@@ -1014,15 +1083,15 @@ __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
     if (i0 >= i1) return;
     if (pass == 2 && st.k == 1) return;  // a unique winner needs no ranks
     const uint32_t *occ = p.big_occ + p.big_ooff[bi];
-    const uint32_t *gk = p.gkey + p.big_toff[bi];
-    const uint32_t *gc = p.gcnt + p.big_toff[bi];
+    const unsigned long long *gt = p.gtab + p.big_toff[bi];
+    const unsigned long long cmask = (1ull << p.hub_cbits) - 1;
     const int W = (pass >= 1) ? st.W : 0;
     const int cmn = (pass == 2) ? st.cmin : 0, cmx = (pass == 2) ? st.cmax : 0;
     int r0 = 0, r1 = (pass == 1) ? INT_MAX : 0, r2 = (pass == 1) ? -1 : 0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
-        const uint32_t sidx = occ[i];
-        const uint32_t k = gk[sidx];
-        const int cnt = (int)gc[sidx];
+        const unsigned long long x = gt[occ[i]];
+        const uint32_t k = (uint32_t)(x >> p.hub_cbits) & p.hub_lmask;
+        const int cnt = (int)(x & cmask);
         if (pass == 0) {
             r0 = max(r0, cnt);
         } else if (pass == 1) {
@@ -1108,8 +1177,8 @@ __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
         } else if (!sq.fail && r == st.rmax) {
             label = st.cmax;
         } else {
-            WarpTableQuery q{p.gkey + p.big_toff[bi], p.gcnt + p.big_toff[bi], (int)p.big_tcap[bi], d, st.W,
-                             st.rmin, st.rmax, hist, lane, pick_scratch};
+            WarpTableQueryT<HubTable> q{{p.gtab + p.big_toff[bi], p.hub_cbits, p.hub_gshift, p.hub_lmask, p.hub_gen},
+                                        (int)p.big_tcap[bi], d, st.W, st.rmin, st.rmax, hist, lane, pick_scratch};
             q.occ = p.big_occ + p.big_ooff[bi];
             q.nocc = d;
             if (sq.fail) r = resolve_rank(a, d, N, v == p.last_v, q);
@@ -1123,25 +1192,6 @@ __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
             atomicAdd(&p.ctl->changes, 1ull);
             if (p.changed) p.changed[atomicAdd(&p.ctl->changed_n, 1)] = v;
         }
-    }
-}
-
-// Empty the occupied slots of every big table (chunks of the occupied lists).
-__global__ void __launch_bounds__(kTB) big_clear_kernel(IterArgs p)
-{
-    if (!ctl_active(p.ctl)) return;
-    if ((int)blockIdx.x >= p.nschunks) return;
-    const int c = p.s0 + blockIdx.x;
-    const int bi = p.schunk_big[c];
-    const int d = p.bstat[bi].d;
-    const int64_t i0 = p.schunk_s0[c], i1 = min(p.schunk_s1[c], (int64_t)d);
-    const uint32_t *occ = p.big_occ + p.big_ooff[bi];
-    uint32_t *gk = p.gkey + p.big_toff[bi];
-    uint32_t *gc = p.gcnt + p.big_toff[bi];
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
-        const uint32_t sidx = occ[i];
-        gk[sidx] = kEmpty;
-        gc[sidx] = 0;
     }
 }
 
