@@ -594,16 +594,18 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
         for (int s = lane; s < cap; s += 32)
             if (key[s] != kEmpty) sum5_add(part, (int)key[s], (int)cnt[s]);
         const Sum5 sm = sum5_warp(part);
-        int rmin = 0, rmax = 0;
+        int rmin = 0, rmax = sm.d - 1;  // when every distinct label is a candidate
         if (sm.k > 1) {
-            int a0 = 0, a1 = 0;
-            for (int s = lane; s < cap; s += 32)
-                if (key[s] != kEmpty) {
-                    a0 += (int)key[s] < sm.mn;
-                    a1 += (int)key[s] < sm.mx;
-                }
-            rmin = __reduce_add_sync(kFull, a0);
-            rmax = __reduce_add_sync(kFull, a1);
+            if (sm.k < sm.d) {
+                int a0 = 0, a1 = 0;
+                for (int s = lane; s < cap; s += 32)
+                    if (key[s] != kEmpty) {
+                        a0 += (int)key[s] < sm.mn;
+                        a1 += (int)key[s] < sm.mx;
+                    }
+                rmin = __reduce_add_sync(kFull, a0);
+                rmax = __reduce_add_sync(kFull, a1);
+            }
             if (sm.k > 2) {  // resolving may need the runs themselves (unsorted)
                 int32_t *rl = p.run_lab + (o0 - p.nbr_shift);
                 uint16_t *rc = p.run_cnt + (o0 - p.nbr_shift);
@@ -725,10 +727,12 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
         }
         __syncthreads();
         const Sum5 s = br.reduce(t64_scan(cta_tab, (int)cap, tid, THREADS, gen));
-        int rmin = 0, rmax = 0;
+        int rmin = 0, rmax = s.d - 1;  // when every distinct label is a candidate
         if (s.k > 1) {
-            t64_ranks(cta_tab, (int)cap, tid, THREADS, gen, s.mn, s.mx, rmin, rmax);
-            br.reduce2(rmin, rmax);
+            if (s.k < s.d) {
+                t64_ranks(cta_tab, (int)cap, tid, THREADS, gen, s.mn, s.mx, rmin, rmax);
+                br.reduce2(rmin, rmax);
+            }
             if (s.k > 2) {
                 if (tid == 0) sctr = 0;
                 __syncthreads();
