@@ -33,7 +33,7 @@ constexpr int kNW = kTB / 32;         // warps per CTA
 constexpr int kTileSlots = 2048;      // shared-memory label slots per tile
 constexpr int kTileV = 512;           // vertices per tile
 constexpr int kSmallMax = 32;         // degree handled by one warp pack
-constexpr int kBigChunk = 4096;       // edges per big_insert CTA
+constexpr int kBigChunk = 1024;       // edges per big_insert CTA
 constexpr int kBigSlotChunk = 8192;   // table slots per big_stats CTA
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
@@ -937,7 +937,7 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
 
 // Count the labels of one chunk of a big vertex's edges in shared memory, then merge
 // the distinct (label, count) pairs into the vertex's global table.
-__global__ void __launch_bounds__(kTB, 3) big_insert_kernel(IterArgs p)
+__global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
 {
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
@@ -991,7 +991,7 @@ __global__ void __launch_bounds__(kTB, 3) big_insert_kernel(IterArgs p)
     int *dcount = &p.bstat[bi].d;
     const int lane = threadIdx.x & 31;
     const uint32_t gen = p.hub_gen;
-    constexpr int U = 4;  // slots per thread with their table reads in flight together
+    constexpr int U = 2;  // slots per thread with their table reads in flight together
     for (int base = 0; base < (int)cap; base += kTB * U) {  // cap is a multiple of kTB * U
         uint32_t L[U], h[U];
         unsigned long long cur[U];
