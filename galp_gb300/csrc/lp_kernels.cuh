@@ -116,6 +116,8 @@ struct IterArgs {
     uint32_t *big_occ;          // occupied-slot list of each big table (capacity = degree)
     const int64_t *big_ooff;    // offset of each big vertex's occupied list
     const int64_t *runbase;     // run base of every vertex when the scan precedes big_resolve
+    int *bpart;                 // per stats chunk: max count, candidates, smallest, largest
+    const int32_t *big_sc0;     // first stats chunk of each big vertex (nbig + 1 entries)
     int32_t *changed;           // frontier mode: vertices whose label changes (else null)
 };
 
@@ -1067,11 +1069,14 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
     }
 }
 
-// Over the occupied slots of each big vertex's table: pass 0 max count; pass 1
-// candidates (count, smallest and largest label); pass 2 ranks of those two labels.
+// Over the occupied slots of each big vertex's table, one CTA per stats chunk.
+// pass 0: the chunk's maximum count, its number of labels of that count and their
+// smallest and largest label -> bpart (big_combine_kernel folds the chunks);
+// pass 2: ranks of the vertex's smallest and largest candidate (only when some but not
+// all distinct labels are candidates).
 __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
 {
-    __shared__ int red[3][kNW];
+    __shared__ int red[4][kNW];
     if (!ctl_active(p.ctl)) return;
     if ((int)blockIdx.x >= p.nschunks) return;
     const int c = p.s0 + blockIdx.x;
@@ -1080,73 +1085,111 @@ __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
     const int d = *((volatile int *)&st.d);
     const int64_t i0 = p.schunk_s0[c];
     const int64_t i1 = min(p.schunk_s1[c], (int64_t)d);
-    if (i0 >= i1) return;
-    if (pass == 2 && st.k == 1) return;  // a unique winner needs no ranks
+    if (pass == 2 && (st.k == 1 || st.k == d || i0 >= i1)) return;
     const uint32_t *occ = p.big_occ + p.big_ooff[bi];
     const unsigned long long *gt = p.gtab + p.big_toff[bi];
     const unsigned long long cmask = (1ull << p.hub_cbits) - 1;
-    const int W = (pass >= 1) ? st.W : 0;
-    const int cmn = (pass == 2) ? st.cmin : 0, cmx = (pass == 2) ? st.cmax : 0;
-    int r0 = 0, r1 = (pass == 1) ? INT_MAX : 0, r2 = (pass == 1) ? -1 : 0;
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
-        const unsigned long long x = gt[occ[i]];
-        const uint32_t k = (uint32_t)(x >> p.hub_cbits) & p.hub_lmask;
-        const int cnt = (int)(x & cmask);
-        if (pass == 0) {
-            r0 = max(r0, cnt);
-        } else if (pass == 1) {
-            if (cnt == W) {
-                r0++;
-                r1 = min(r1, (int)k);
-                r2 = max(r2, (int)k);
-            }
-        } else {
-            r0 += (int)k < cmn;
-            r1 += (int)k < cmx;
-        }
-    }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (pass == 0) {
-        r0 = __reduce_max_sync(kFull, r0);
-    } else if (pass == 1) {
-        r0 = __reduce_add_sync(kFull, r0);
-        r1 = __reduce_min_sync(kFull, r1);
-        r2 = __reduce_max_sync(kFull, r2);
-    } else {
-        r0 = __reduce_add_sync(kFull, r0);
-        r1 = __reduce_add_sync(kFull, r1);
+        int W = 0, k = 0, mn = INT_MAX, mx = -1;
+        for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
+            const unsigned long long x = gt[occ[i]];
+            const int lab = (int)((uint32_t)(x >> p.hub_cbits) & p.hub_lmask), cnt = (int)(x & cmask);
+            if (cnt > W) {
+                W = cnt;
+                k = 1;
+                mn = mx = lab;
+            } else if (cnt == W) {
+                k++;
+                mn = min(mn, lab);
+                mx = max(mx, lab);
+            }
+        }
+        const int Ww = __reduce_max_sync(kFull, W);
+        const bool top = W == Ww;
+        const int kw = __reduce_add_sync(kFull, top ? k : 0);
+        const int mnw = __reduce_min_sync(kFull, top ? mn : INT_MAX);
+        const int mxw = __reduce_max_sync(kFull, top ? mx : -1);
+        if (lane == 0) {
+            red[0][warp] = Ww;
+            red[1][warp] = kw;
+            red[2][warp] = mnw;
+            red[3][warp] = mxw;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int Wb = 0, kb = 0, mnb = INT_MAX, mxb = -1;
+            for (int w = 0; w < kNW; ++w) Wb = max(Wb, red[0][w]);
+            for (int w = 0; w < kNW; ++w)
+                if (red[0][w] == Wb) {
+                    kb += red[1][w];
+                    mnb = min(mnb, red[2][w]);
+                    mxb = max(mxb, red[3][w]);
+                }
+            int *o = p.bpart + 4 * (int64_t)c;
+            o[0] = Wb;
+            o[1] = kb;
+            o[2] = mnb;
+            o[3] = mxb;
+        }
+        return;
     }
+    const int cmn = st.cmin, cmx = st.cmax;
+    int r0 = 0, r1 = 0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
+        const int lab = (int)((uint32_t)(gt[occ[i]] >> p.hub_cbits) & p.hub_lmask);
+        r0 += lab < cmn;
+        r1 += lab < cmx;
+    }
+    r0 = __reduce_add_sync(kFull, r0);
+    r1 = __reduce_add_sync(kFull, r1);
     if (lane == 0) {
         red[0][warp] = r0;
         red[1][warp] = r1;
-        red[2][warp] = r2;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        int a0 = red[0][0], a1 = red[1][0], a2 = red[2][0];
-        for (int w = 1; w < kNW; ++w) {
-            if (pass == 0) {
-                a0 = max(a0, red[0][w]);
-            } else if (pass == 1) {
-                a0 += red[0][w];
-                a1 = min(a1, red[1][w]);
-                a2 = max(a2, red[2][w]);
-            } else {
-                a0 += red[0][w];
-                a1 += red[1][w];
+        int a0 = 0, a1 = 0;
+        for (int w = 0; w < kNW; ++w) {
+            a0 += red[0][w];
+            a1 += red[1][w];
+        }
+        atomicAdd(&st.rmin, a0);
+        atomicAdd(&st.rmax, a1);
+    }
+}
+
+// One thread per big vertex: fold its stats chunks' partial summaries; when every
+// distinct label is a candidate the ranks are 0 and d - 1.
+__global__ void big_combine_kernel(IterArgs p)
+{
+    if (!ctl_active(p.ctl)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.nbig; i += gridDim.x * blockDim.x) {
+        const int bi = p.b0 + i;
+        BigStat &st = p.bstat[bi];
+        const int d = st.d;
+        int W = 0, k = 0, mn = INT_MAX, mx = -1;
+        for (int c = p.big_sc0[bi]; c < p.big_sc0[bi + 1]; ++c) {
+            if (p.schunk_s0[c] >= d) break;  // chunks past the occupied list wrote nothing
+            const int *o = p.bpart + 4 * (int64_t)c;
+            if (o[0] > W) {
+                W = o[0];
+                k = o[1];
+                mn = o[2];
+                mx = o[3];
+            } else if (o[0] == W) {
+                k += o[1];
+                mn = min(mn, o[2]);
+                mx = max(mx, o[3]);
             }
         }
-        if (pass == 0) {
-            atomicMax(&st.W, a0);
-        } else if (pass == 1) {
-            if (a0) {
-                atomicAdd(&st.k, a0);
-                atomicMin(&st.cmin, a1);
-                atomicMax(&st.cmax, a2);
-            }
-        } else {
-            atomicAdd(&st.rmin, a0);
-            atomicAdd(&st.rmax, a1);
+        st.W = W;
+        st.k = k;
+        st.cmin = mn;
+        st.cmax = mx;
+        if (k == d) {
+            st.rmin = 0;
+            st.rmax = d - 1;
         }
     }
 }
