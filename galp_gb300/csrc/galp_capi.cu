@@ -169,9 +169,9 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             const int64_t deg = off[v + 1] - off[v];
             const int32_t b = (int32_t)S.big_v.size();
             S.big_v.push_back(v);
-            S.big_sc0.push_back((int32_t)S.schunk_big.size());
-            uint32_t cap = 1;
-            while ((int64_t)cap < 2 * deg) cap <<= 1;
+            S.big_c0.push_back((int32_t)S.chunk_big.size());
+            // load <= 1/2; a multiple of four slots keeps every table on 32-byte sectors
+            const uint32_t cap = (uint32_t)std::min<int64_t>((2 * deg + 3) & ~(int64_t)3, 0xFFFFFFFCll);
             S.big_toff.push_back(toff);
             S.big_tcap.push_back(cap);
             S.big_ooff.push_back(ooff);
@@ -203,7 +203,7 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         S.max_scope_vertices = std::max(S.max_scope_vertices, sc.v1 - sc.v0);
         S.scopes.push_back(sc);
     }
-    S.big_sc0.push_back((int32_t)S.schunk_big.size());
+    S.big_c0.push_back((int32_t)S.chunk_big.size());
     return true;
 }
 
@@ -321,8 +321,8 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     if ((rc = upload(b_schunk_big, d_schunk_big, sched.schunk_big, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s0, d_schunk_s0, sched.schunk_s0, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s1, d_schunk_s1, sched.schunk_s1, st, h2d))) return rc;
-    if ((rc = upload(b_big_sc0, d_big_sc0, sched.big_sc0, st, h2d))) return rc;
-    GALP_CUDA(b_bpart.alloc(sizeof(int) * 4 * std::max<size_t>(sched.schunk_big.size(), 1)));
+    if ((rc = upload(b_big_c0, d_big_c0, sched.big_c0, st, h2d))) return rc;
+    GALP_CUDA(b_bpart.alloc(sizeof(int) * 4 * std::max<size_t>(sched.chunk_big.size(), 1)));
     // per-vertex state, spill and tied lists
     const size_t nn = (size_t)std::max<int64_t>(n, 1);
     GALP_CUDA(b_dcnt.alloc(sizeof(int32_t) * nn));
@@ -499,7 +499,7 @@ IterArgs Engine::big_args(const Scope &sc) const
     a.schunk_big = d_schunk_big;
     a.schunk_s0 = d_schunk_s0;
     a.schunk_s1 = d_schunk_s1;
-    a.big_sc0 = d_big_sc0;
+    a.big_c0 = d_big_c0;
     a.bpart = (int *)b_bpart.p;
     a.nschunks = sc.ns;
     a.gtab = (unsigned long long *)b_gtab.p;
@@ -625,11 +625,9 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         if (prof.on) e0 = prof.mark(st);
         big_insert_kernel<<<a.nchunks, kTB, 0, st>>>(a);
         launched("big_insert_kernel", st);
-        big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a, 0);
-        launched("big_stats_kernel", st);
-        big_combine_kernel<<<(a.nbig + 255) / 256, 256, 0, st>>>(a);
+        big_combine_kernel<<<(a.nbig + 7) / 8, 256, 0, st>>>(a);
         launched("big_combine_kernel", st);
-        big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a, 2);
+        big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a);
         launched("big_stats_kernel", st);
         big_dcnt_kernel<<<(a.nbig + 255) / 256, 256, 0, st>>>(a, q.dcnt);
         launched("big_dcnt_kernel", st);

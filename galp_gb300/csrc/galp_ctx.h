@@ -66,12 +66,12 @@ struct Schedule {
     std::vector<int32_t> mid_deg;    // degree of each mid_v entry
     std::vector<int32_t> big_v;      // vertex of each big entry
     std::vector<int64_t> big_toff;   // table offset, relative to its scope
-    std::vector<uint32_t> big_tcap;  // table capacity (power of two >= 2 * degree)
+    std::vector<uint32_t> big_tcap;  // table capacity (>= 2 * degree, a multiple of 4)
     std::vector<int64_t> big_ooff;   // occupied-list offset, relative to its scope
     std::vector<int32_t> chunk_big;
     std::vector<int64_t> chunk_e0, chunk_e1;
     std::vector<int32_t> schunk_big;
-    std::vector<int32_t> big_sc0;    // first stats chunk of each big vertex, then the total
+    std::vector<int32_t> big_c0;     // first insert chunk of each big vertex, then the total
     std::vector<int64_t> schunk_s0, schunk_s1;
     std::vector<Scope> scopes;
     int64_t max_table_slots = 0, max_occ_slots = 0, max_scope_edges = 0, m_big = 0;
@@ -175,7 +175,7 @@ struct Engine {
     bool registered = false;         // the library pinned h_nbr
     Schedule sched;
     DevBuf b_nbr[2], b_off, b_pack_v0, b_pack_nv, b_mid_v, b_big_v, b_big_toff, b_big_tcap;
-    DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff, b_big_sc0, b_bpart;
+    DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff, b_big_c0, b_bpart;
     DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_gtab, b_occ, b_bad;
     DevBuf b_dcnt, b_runbase, b_c0, b_c1, b_kw, b_r, b_run_lab, b_run_cnt, b_tsmall, b_tmid, b_bsum;
     DevBuf b_dirty, b_changed, b_chk;  // frontier mode; setup adjacency checks
@@ -196,7 +196,7 @@ struct Engine {
     int64_t *d_chunk_e0 = nullptr, *d_chunk_e1 = nullptr;
     int32_t *d_schunk_big = nullptr;
     int64_t *d_schunk_s0 = nullptr, *d_schunk_s1 = nullptr;
-    int32_t *d_big_sc0 = nullptr;
+    int32_t *d_big_c0 = nullptr;
     int sms = 1;
     bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
     bool symmetric = false;   // edge multiset symmetric (frontier marking along out-edges)

@@ -3,7 +3,7 @@
 // One iteration over a scope (whole graph in-core, one batch out-of-core, one graph
 // of a batch) is:
 //
-//   big_insert  -> big_stats x3 -> lp_tile_kernel -> big_resolve -> big_clear -> finalize
+//   big_insert -> big_combine -> [big_stats] -> lp_tile_kernel -> big_resolve -> finalize
 //
 // lp_tile_kernel is a persistent, single-pass kernel: CTAs take vertex tiles in
 // vertex order from an atomic ticket, gather the tile's neighbour labels into shared
@@ -13,7 +13,7 @@
 // decoupled look-back over the preceding tiles, and resolve every vertex's winner
 // with the positional tie rule while the tile is still on chip.  Vertices of degree
 // above kTileSlots ("big") are counted beforehand into global hash tables by
-// big_insert/big_stats, take part in the scan as single-vertex tiles, and are
+// big_insert/big_combine (big_stats adds candidate ranks), take part in the scan as single-vertex tiles, and are
 // resolved by big_resolve once their run base is known.
 //
 // Reference counterparts: DPPBase::perform_lp (label_propagation/src/dpp/dpp.cuh:104-138),
@@ -97,7 +97,7 @@ struct IterArgs {
     int32_t nbig;
     const int32_t *big_v;       // vertex of each big entry
     const int64_t *big_toff;    // table offset of each big entry
-    const uint32_t *big_tcap;   // table capacity (power of two)
+    const uint32_t *big_tcap;   // table capacity (>= 2 * degree)
     const int32_t *chunk_big;   // insert chunk -> big index
     const int64_t *chunk_e0;    // insert chunk -> first edge
     const int64_t *chunk_e1;    // insert chunk -> end edge
@@ -116,8 +116,8 @@ struct IterArgs {
     uint32_t *big_occ;          // occupied-slot list of each big table (capacity = degree)
     const int64_t *big_ooff;    // offset of each big vertex's occupied list
     const int64_t *runbase;     // run base of every vertex when the scan precedes big_resolve
-    int *bpart;                 // per stats chunk: max count, candidates, smallest, largest
-    const int32_t *big_sc0;     // first stats chunk of each big vertex (nbig + 1 entries)
+    int *bpart;                 // per insert chunk: max count, candidates, smallest, largest
+    const int32_t *big_c0;      // first insert chunk of each big vertex (nbig + 1 entries)
     int32_t *changed;           // frontier mode: vertices whose label changes (else null)
 };
 
@@ -943,16 +943,19 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
 {
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
+    __shared__ uint16_t sused[kBigChunk];  // occupied local slots, compacted
+    __shared__ int nused;
     if (!ctl_active(p.ctl)) return;
     if ((int)blockIdx.x >= p.nchunks) return;
-    const int c = p.c0 + blockIdx.x;
-    const int bi = p.chunk_big[c];
-    const int64_t e0 = p.chunk_e0[c] - p.nbr_shift, e1 = p.chunk_e1[c] - p.nbr_shift;
+    const int ch = p.c0 + blockIdx.x;
+    const int bi = p.chunk_big[ch];
+    const int64_t e0 = p.chunk_e0[ch] - p.nbr_shift, e1 = p.chunk_e1[ch] - p.nbr_shift;
     const uint32_t cap = 2u * kBigChunk;
     for (int s = threadIdx.x; s < (int)cap; s += kTB) {
         skey[s] = kEmpty;
         scnt[s] = 0;
     }
+    if (threadIdx.x == 0) nused = 0;
     __syncthreads();
     {
         // all of a thread's neighbour loads, then all its label gathers, in flight together
@@ -982,24 +985,57 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
         }
     }
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // compact the occupied local slots, so the merge rounds below run on full warps
+    for (int s0 = 0; s0 < (int)cap; s0 += kTB) {
+        const int s = s0 + threadIdx.x;
+        const bool used = skey[s] != kEmpty;
+        const unsigned m = __ballot_sync(kFull, used);
+        if (!m) continue;
+        int at = 0;
+        if (lane == __ffs(m) - 1) at = atomicAdd(&nused, __popc(m));
+        at = __shfl_sync(kFull, at, __ffs(m) - 1);
+        if (used) sused[at + __popc(m & ((1u << lane) - 1))] = (uint16_t)s;
+    }
+    __syncthreads();
+    const int nloc = nused;
     // Merge into the vertex's global table of generation-tagged 64-bit slots: a slot of
     // another generation is free, so tables are never cleared between iterations.  The
     // count is the low field; a 32-bit add on the slot's low word never carries into the
-    // label (a count stays below 2^hub_cbits).
+    // label (a count stays below 2^hub_cbits).  Every merge observes the label's count
+    // right after it (the claim: its own count; an add: the returned old count plus its
+    // own); the last merge of a label observes its final count, so the observations fold
+    // into the vertex's maximum count, candidates and their extreme labels
+    // (big_combine_kernel folds the chunks) without a pass over the table.
     const int64_t toff = p.big_toff[bi];
     const uint32_t gcap = p.big_tcap[bi];
     unsigned long long *gt = p.gtab + toff;
     uint32_t *occ = p.big_occ + p.big_ooff[bi];
     int *dcount = &p.bstat[bi].d;
-    const int lane = threadIdx.x & 31;
     const uint32_t gen = p.hub_gen;
+    const uint32_t cmask = (1u << p.hub_cbits) - 1u;  // hub_cbits <= 31
+    int oW = 0, ok = 0, omn = INT_MAX, omx = -1;      // observations of this thread
+    auto observe = [&](uint32_t L, uint32_t now) {
+        const int x = (int)now;
+        if (x > oW) {
+            oW = x;
+            ok = 1;
+            omn = omx = (int)L;
+        } else if (x == oW) {
+            ok++;
+            omn = min(omn, (int)L);
+            omx = max(omx, (int)L);
+        }
+    };
     constexpr int U = 2;  // slots per thread with their table reads in flight together
-    for (int base = 0; base < (int)cap; base += kTB * U) {  // cap is a multiple of kTB * U
-        uint32_t L[U], h[U];
+    for (int base = 0; base < nloc; base += kTB * U) {  // block-uniform trip count
+        uint32_t L[U], h[U], ls[U];
         unsigned long long cur[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            L[u] = skey[base + u * kTB + threadIdx.x];
+            const int i = base + u * kTB + threadIdx.x;
+            ls[u] = i < nloc ? sused[i] : 0u;
+            L[u] = i < nloc ? skey[ls[u]] : kEmpty;
             h[u] = (L[u] != kEmpty) ? hslot(L[u], gcap) : 0;
         }
 #pragma unroll
@@ -1013,10 +1049,10 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
         for (int u = 0; u < U; ++u) {
             state[u] = 0;
             if (L[u] == kEmpty) continue;
-            c[u] = scnt[base + u * kTB + threadIdx.x];
+            c[u] = scnt[ls[u]];
             tag[u] = ((unsigned long long)gen << p.hub_gshift) | ((unsigned long long)L[u] << p.hub_cbits);
             if ((cur[u] >> p.hub_cbits) == (tag[u] >> p.hub_cbits)) {  // same generation and label
-                atomicAdd((unsigned int *)&gt[h[u]], c[u]);
+                observe(L[u], (atomicAdd((unsigned int *)&gt[h[u]], c[u]) & cmask) + c[u]);
                 state[u] = 1;
             } else {
                 state[u] = (uint32_t)(cur[u] >> p.hub_gshift) != gen ? 2 : 3;
@@ -1040,7 +1076,7 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
             if (state[u] == 3) {  // the slot changed or belongs to another label
                 for (;;) {
                     if ((cur[u] >> p.hub_cbits) == (tag[u] >> p.hub_cbits)) {
-                        atomicAdd((unsigned int *)&gt[h[u]], c[u]);
+                        observe(L[u], (atomicAdd((unsigned int *)&gt[h[u]], c[u]) & cmask) + c[u]);
                         break;
                     }
                     if ((uint32_t)(cur[u] >> p.hub_gshift) != gen) {  // free: claim it
@@ -1057,6 +1093,7 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
                     cur[u] = *(volatile unsigned long long *)&gt[h[u]];
                 }
             }
+            if (created) observe(L[u], c[u]);
             // record newly occupied slots in the vertex's occupied list (warp-aggregated)
             const unsigned m = __ballot_sync(kFull, created);
             if (m) {
@@ -1067,16 +1104,46 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
             }
         }
     }
+    // the chunk's partial summary -> bpart (the key arrays are no longer read: reuse)
+    {
+        const int Ww = __reduce_max_sync(kFull, oW);
+        const bool top = oW == Ww;
+        const int kw = __reduce_add_sync(kFull, top ? ok : 0);
+        const int mnw = __reduce_min_sync(kFull, top ? omn : INT_MAX);
+        const int mxw = __reduce_max_sync(kFull, top ? omx : -1);
+        __syncthreads();
+        int *red = reinterpret_cast<int *>(skey);
+        if (lane == 0) {
+            red[warp] = Ww;
+            red[kNW + warp] = kw;
+            red[2 * kNW + warp] = mnw;
+            red[3 * kNW + warp] = mxw;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int Wb = 0, kb = 0, mnb = INT_MAX, mxb = -1;
+            for (int w = 0; w < kNW; ++w) Wb = max(Wb, red[w]);
+            for (int w = 0; w < kNW; ++w)
+                if (red[w] == Wb) {
+                    kb += red[kNW + w];
+                    mnb = min(mnb, red[2 * kNW + w]);
+                    mxb = max(mxb, red[3 * kNW + w]);
+                }
+            int *o = p.bpart + 4 * (int64_t)ch;
+            o[0] = Wb;
+            o[1] = kb;
+            o[2] = mnb;
+            o[3] = mxb;
+        }
+    }
 }
 
-// Over the occupied slots of each big vertex's table, one CTA per stats chunk.
-// pass 0: the chunk's maximum count, its number of labels of that count and their
-// smallest and largest label -> bpart (big_combine_kernel folds the chunks);
-// pass 2: ranks of the vertex's smallest and largest candidate (only when some but not
-// all distinct labels are candidates).
-__global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
+// Ranks of each big vertex's smallest and largest candidate among its distinct labels,
+// over the occupied slots of its table, one CTA per stats chunk; only vertices with
+// some but not all distinct labels tied at the maximum need them.
+__global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p)
 {
-    __shared__ int red[4][kNW];
+    __shared__ int red[2][kNW];
     if (!ctl_active(p.ctl)) return;
     if ((int)blockIdx.x >= p.nschunks) return;
     const int c = p.s0 + blockIdx.x;
@@ -1085,55 +1152,10 @@ __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
     const int d = *((volatile int *)&st.d);
     const int64_t i0 = p.schunk_s0[c];
     const int64_t i1 = min(p.schunk_s1[c], (int64_t)d);
-    if (pass == 2 && (st.k == 1 || st.k == d || i0 >= i1)) return;
+    if (st.k == 1 || st.k == d || i0 >= i1) return;
     const uint32_t *occ = p.big_occ + p.big_ooff[bi];
     const unsigned long long *gt = p.gtab + p.big_toff[bi];
-    const unsigned long long cmask = (1ull << p.hub_cbits) - 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (pass == 0) {
-        int W = 0, k = 0, mn = INT_MAX, mx = -1;
-        for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
-            const unsigned long long x = gt[occ[i]];
-            const int lab = (int)((uint32_t)(x >> p.hub_cbits) & p.hub_lmask), cnt = (int)(x & cmask);
-            if (cnt > W) {
-                W = cnt;
-                k = 1;
-                mn = mx = lab;
-            } else if (cnt == W) {
-                k++;
-                mn = min(mn, lab);
-                mx = max(mx, lab);
-            }
-        }
-        const int Ww = __reduce_max_sync(kFull, W);
-        const bool top = W == Ww;
-        const int kw = __reduce_add_sync(kFull, top ? k : 0);
-        const int mnw = __reduce_min_sync(kFull, top ? mn : INT_MAX);
-        const int mxw = __reduce_max_sync(kFull, top ? mx : -1);
-        if (lane == 0) {
-            red[0][warp] = Ww;
-            red[1][warp] = kw;
-            red[2][warp] = mnw;
-            red[3][warp] = mxw;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int Wb = 0, kb = 0, mnb = INT_MAX, mxb = -1;
-            for (int w = 0; w < kNW; ++w) Wb = max(Wb, red[0][w]);
-            for (int w = 0; w < kNW; ++w)
-                if (red[0][w] == Wb) {
-                    kb += red[1][w];
-                    mnb = min(mnb, red[2][w]);
-                    mxb = max(mxb, red[3][w]);
-                }
-            int *o = p.bpart + 4 * (int64_t)c;
-            o[0] = Wb;
-            o[1] = kb;
-            o[2] = mnb;
-            o[3] = mxb;
-        }
-        return;
-    }
     const int cmn = st.cmin, cmx = st.cmax;
     int r0 = 0, r1 = 0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
@@ -1159,37 +1181,44 @@ __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p, int pass)
     }
 }
 
-// One thread per big vertex: fold its stats chunks' partial summaries; when every
+// One warp per big vertex: fold its insert chunks' partial summaries; when every
 // distinct label is a candidate the ranks are 0 and d - 1.
 __global__ void big_combine_kernel(IterArgs p)
 {
     if (!ctl_active(p.ctl)) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < p.nbig; i += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.nbig; i += nw) {
         const int bi = p.b0 + i;
-        BigStat &st = p.bstat[bi];
-        const int d = st.d;
         int W = 0, k = 0, mn = INT_MAX, mx = -1;
-        for (int c = p.big_sc0[bi]; c < p.big_sc0[bi + 1]; ++c) {
-            if (p.schunk_s0[c] >= d) break;  // chunks past the occupied list wrote nothing
-            const int *o = p.bpart + 4 * (int64_t)c;
-            if (o[0] > W) {
-                W = o[0];
-                k = o[1];
-                mn = o[2];
-                mx = o[3];
-            } else if (o[0] == W) {
-                k += o[1];
-                mn = min(mn, o[2]);
-                mx = max(mx, o[3]);
+        for (int c = p.big_c0[bi] + lane; c < p.big_c0[bi + 1]; c += 32) {
+            const int4 o = *reinterpret_cast<const int4 *>(p.bpart + 4 * (int64_t)c);
+            if (o.x > W) {
+                W = o.x;
+                k = o.y;
+                mn = o.z;
+                mx = o.w;
+            } else if (o.x == W) {
+                k += o.y;
+                mn = min(mn, o.z);
+                mx = max(mx, o.w);
             }
         }
-        st.W = W;
-        st.k = k;
-        st.cmin = mn;
-        st.cmax = mx;
-        if (k == d) {
-            st.rmin = 0;
-            st.rmax = d - 1;
+        const int Ww = __reduce_max_sync(kFull, W);
+        const bool top = W == Ww;
+        k = __reduce_add_sync(kFull, top ? k : 0);
+        mn = __reduce_min_sync(kFull, top ? mn : INT_MAX);
+        mx = __reduce_max_sync(kFull, top ? mx : -1);
+        if (lane == 0) {
+            BigStat &st = p.bstat[bi];
+            st.W = Ww;
+            st.k = k;
+            st.cmin = mn;
+            st.cmax = mx;
+            if (k == st.d) {
+                st.rmin = 0;
+                st.rmax = st.d - 1;
+            }
         }
     }
 }

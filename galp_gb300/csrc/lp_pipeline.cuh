@@ -377,9 +377,10 @@ __device__ __forceinline__ unsigned long long t64_tag(uint32_t gen, uint32_t lab
     return ((unsigned long long)gen << kT64GenShift) | ((unsigned long long)label << 14);
 }
 
-// Returns the slot index when this insert claimed a new slot, else -1.
-__device__ __forceinline__ int t64_insert(unsigned long long *tab, uint32_t cap, uint32_t gen, uint32_t label,
-                                          uint32_t c)
+// Adds c occurrences of label.  Returns the label's count right after this insert and
+// sets `claimed` when the insert took a new slot (the label's first insert).
+__device__ __forceinline__ uint32_t t64_insert(unsigned long long *tab, uint32_t cap, uint32_t gen, uint32_t label,
+                                               uint32_t c, bool &claimed)
 {
     const unsigned long long tag = t64_tag(gen, label);
     uint32_t h = hslot(label, cap);
@@ -388,12 +389,15 @@ __device__ __forceinline__ int t64_insert(unsigned long long *tab, uint32_t cap,
         if ((cur & ~kT64CntMask) == tag) {
             // the count is the low 14 bits of the low word (little-endian), and the total
             // stays below 2^14: a 32-bit add never carries into the label
-            atomicAdd((unsigned int *)&tab[h], c);
-            return -1;
+            claimed = false;
+            return (atomicAdd((unsigned int *)&tab[h], c) & (uint32_t)kT64CntMask) + c;
         }
         if ((uint32_t)(cur >> kT64GenShift) != gen) {  // stale: claim it
             const unsigned long long prev = atomicCAS(&tab[h], cur, tag | c);
-            if (prev == cur) return (int)h;
+            if (prev == cur) {
+                claimed = true;
+                return c;
+            }
             cur = prev;  // taken meanwhile: look at it again
             continue;
         }
@@ -410,9 +414,13 @@ struct Sum5 {
 
 __device__ __forceinline__ Sum5 sum5_empty() { return Sum5{0, 0, 0, INT_MAX, -1}; }
 
-__device__ __forceinline__ void sum5_add(Sum5 &s, int lab, int c)
+// Fold the count a label has right after one of its inserts (d is left to the caller).
+// The counts a label passes through rise strictly and its last insert sees its final
+// count, so folding every insert of a vertex gives its maximum count W, the number k
+// of labels that reach W (each sees W exactly once) and their smallest and largest
+// label, with no pass over the table; d is the number of slot claims.
+__device__ __forceinline__ void sum5_observe(Sum5 &s, int lab, int c)
 {
-    s.d++;
     if (c > s.W) {
         s.W = c;
         s.k = 1;
@@ -434,17 +442,6 @@ __device__ __forceinline__ Sum5 sum5_warp(const Sum5 &s)
     r.mn = __reduce_min_sync(kFull, top ? s.mn : INT_MAX);
     r.mx = __reduce_max_sync(kFull, top ? s.mx : -1);
     return r;
-}
-
-// Scan slots [t0, cap) step `stride` of the current generation into a partial summary.
-__device__ __forceinline__ Sum5 t64_scan(const unsigned long long *tab, int cap, int t0, int stride, uint32_t gen)
-{
-    Sum5 s = sum5_empty();
-    for (int i = t0; i < cap; i += stride) {
-        const unsigned long long x = tab[i];
-        if ((uint32_t)(x >> kT64GenShift) == gen) sum5_add(s, (int)((x >> 14) & 0x7FFFFFFF), (int)(x & kT64CntMask));
-    }
-    return s;
 }
 
 // Ranks of cmin and cmax among the vertex's distinct labels (partial counts).
@@ -486,16 +483,23 @@ __device__ __forceinline__ void t64_spill(const unsigned long long *tab, int cap
 }
 
 // Insert one row of gathered labels: lanes holding the same label add once when
-// `aggregate` (heavy labels would otherwise serialise on one slot).
+// `aggregate` (heavy labels would otherwise serialise on one slot).  Each insert's
+// observed count folds into `obs`; obs.d counts the claims.
 __device__ __forceinline__ void t64_insert_row(unsigned long long *tab, uint32_t cap, uint32_t gen, uint32_t lb,
-                                               bool aggregate)
+                                               bool aggregate, Sum5 &obs)
 {
+    uint32_t c = 1;
+    bool mine = lb != kEmpty;
     if (aggregate) {
         const unsigned same = __match_any_sync(kFull, lb);
-        const int lane = threadIdx.x & 31;
-        if (lb != kEmpty && lane == __ffs(same) - 1) t64_insert(tab, cap, gen, lb, (uint32_t)__popc(same));
-    } else if (lb != kEmpty) {
-        t64_insert(tab, cap, gen, lb, 1u);
+        mine = mine && (int)(threadIdx.x & 31) == __ffs(same) - 1;
+        c = (uint32_t)__popc(same);
+    }
+    if (mine) {
+        bool claimed;
+        const uint32_t now = t64_insert(tab, cap, gen, lb, c, claimed);
+        obs.d += claimed;
+        sum5_observe(obs, (int)lb, (int)now);
     }
 }
 
@@ -573,26 +577,26 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
         uint32_t lb[PER];
 #pragma unroll
         for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[u]]) : kEmpty;
+        Sum5 part = sum5_empty();  // observed counts (sum5_observe); d = claims
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
             if (u * 32 >= deg) break;  // warp-uniform
             // lanes holding the same label add once (heavy labels would serialise)
             const unsigned same = __match_any_sync(kFull, lb[u]);
             if (lb[u] == kEmpty || lane != __ffs(same) - 1) continue;
+            const uint32_t c = (uint32_t)__popc(same);
             uint32_t h = hslot(lb[u], (uint32_t)cap);
             for (;;) {
                 const uint32_t prev = atomicCAS(&key[h], kEmpty, lb[u]);
                 if (prev == kEmpty || prev == lb[u]) {
-                    atomicAdd(&cnt[h], (uint32_t)__popc(same));
+                    part.d += prev == kEmpty;
+                    sum5_observe(part, (int)lb[u], (int)(atomicAdd(&cnt[h], c) + c));
                     break;
                 }
                 h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
             }
         }
         __syncwarp();
-        Sum5 part = sum5_empty();
-        for (int s = lane; s < cap; s += 32)
-            if (key[s] != kEmpty) sum5_add(part, (int)key[s], (int)cnt[s]);
         const Sum5 sm = sum5_warp(part);
         int rmin = 0, rmax = sm.d - 1;  // when every distinct label is a candidate
         if (sm.k > 1) {
@@ -707,6 +711,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
         const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
         const uint32_t cap = 2 * pad32(deg);
         const bool agg = use_aggregation(p, v, deg);
+        Sum5 obs = sum5_empty();
         // gather in rounds of PER loads per thread in flight together
         constexpr int PER = 8;
         for (int base = 0; base < deg; base += THREADS * PER) {
@@ -722,11 +727,11 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
 #pragma unroll
             for (int u = 0; u < PER; ++u) {
                 if (base + u * THREADS >= deg) break;  // block-uniform
-                t64_insert_row(cta_tab, cap, gen, lb[u], agg);
+                t64_insert_row(cta_tab, cap, gen, lb[u], agg, obs);
             }
         }
-        __syncthreads();
-        const Sum5 s = br.reduce(t64_scan(cta_tab, (int)cap, tid, THREADS, gen));
+        // the reduction's barrier also completes the table for the rank and spill passes
+        const Sum5 s = br.reduce(obs);
         int rmin = 0, rmax = s.d - 1;  // when every distinct label is a candidate
         if (s.k > 1) {
             if (s.k < s.d) {
