@@ -37,6 +37,20 @@ __device__ __forceinline__ uint32_t hslot(uint32_t x, uint32_t cap)
     return __umulhi(mix32(x), cap);
 }
 
+// Neighbour IDs are read once per iteration: the streaming hint (evict first in L1 and
+// L2) keeps them from pushing the label array, read at random, out of L2.
+__device__ __forceinline__ int32_t ld_nbr(const int32_t *p) { return __ldcs(p); }
+
+// Label gathers: the L2 evict-last policy keeps the label array (read at random, and
+// again in the next iteration) resident ahead of streamed and written data.
+__device__ __forceinline__ int32_t ld_label(const int32_t *p)
+{
+    int32_t v;
+    asm("{\n\t.reg .b64 pol;\n\tcreatepolicy.fractional.L2::evict_last.b64 pol, 1.0;\n\t"
+        "ld.global.nc.L2::cache_hint.b32 %0, [%1], pol;\n\t}" : "=r"(v) : "l"(p));
+    return v;
+}
+
 // ----- relaxed 64-bit global accesses for the look-back status words -----
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p)
 {

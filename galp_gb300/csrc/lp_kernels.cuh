@@ -964,11 +964,11 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const int64_t e = e0 + threadIdx.x + (int64_t)i * kTB;
-            nb[i] = (e < e1) ? __ldg(&p.nbr[e]) : -1;
+            nb[i] = (e < e1) ? ld_nbr(&p.nbr[e]) : -1;
         }
         uint32_t lb[PER];
 #pragma unroll
-        for (int i = 0; i < PER; ++i) lb[i] = (nb[i] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[i]]) : kEmpty;
+        for (int i = 0; i < PER; ++i) lb[i] = (nb[i] >= 0) ? (uint32_t)ld_label(&p.lab_in[nb[i]]) : kEmpty;
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const uint32_t L = lb[i];

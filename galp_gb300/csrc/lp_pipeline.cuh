@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(256, 6) count_small_kernel(PipeArgs p)
         const int seg_last = valid ? (later_start ? __ffs(later_start) - 2 : total - 1) : lane;
         const int64_t oj = obase + j;  // the owner's first CSR entry
         int lab = 0;
-        if (valid) lab = __ldg(&p.lab_in[__ldg(&p.nbr[obase + lane - p.nbr_shift])]);
+        if (valid) lab = ld_label(&p.lab_in[ld_nbr(&p.nbr[obase + lane - p.nbr_shift])]);
         const unsigned vm = valid ? (((seg_last == 31) ? kFull : ((2u << seg_last) - 1u)) & ~((1u << j) - 1u))
                                   : (1u << lane);
         if (p.small_sort && p.lab27) {
@@ -572,11 +572,11 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
             const int e = lane + u * 32;
-            nb[u] = (e < deg) ? __ldg(&p.nbr[o0 + e - p.nbr_shift]) : -1;
+            nb[u] = (e < deg) ? ld_nbr(&p.nbr[o0 + e - p.nbr_shift]) : -1;
         }
         uint32_t lb[PER];
 #pragma unroll
-        for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[u]]) : kEmpty;
+        for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)ld_label(&p.lab_in[nb[u]]) : kEmpty;
         Sum5 part = sum5_empty();  // observed counts (sum5_observe); d = claims
 #pragma unroll
         for (int u = 0; u < PER; ++u) {
@@ -719,11 +719,11 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
 #pragma unroll
             for (int u = 0; u < PER; ++u) {
                 const int e = base + tid + u * THREADS;
-                nb[u] = (e < deg) ? __ldg(&p.nbr[o0 + e - p.nbr_shift]) : -1;
+                nb[u] = (e < deg) ? ld_nbr(&p.nbr[o0 + e - p.nbr_shift]) : -1;
             }
             uint32_t lb[PER];
 #pragma unroll
-            for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[u]]) : kEmpty;
+            for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)ld_label(&p.lab_in[nb[u]]) : kEmpty;
 #pragma unroll
             for (int u = 0; u < PER; ++u) {
                 if (base + u * THREADS >= deg) break;  // block-uniform
