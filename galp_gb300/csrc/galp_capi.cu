@@ -645,11 +645,11 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
                            32 * kMidWarps, 0, st>>>(q);
         launched("count_mid_kernel", st);
         count_cta_kernel<128, 2 * kLargeAMax>
-            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 12)), 128,
+            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 10)), 128,
                sizeof(unsigned long long) * 2 * kLargeAMax, st>>>(q, 0);
         launched("count_cta_kernel<128>", st);
         count_cta_kernel<kTB, 2 * kLargeMax>
-            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * 6)), kTB,
+            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * 5)), kTB,
                sizeof(unsigned long long) * 2 * kLargeMax, st>>>(q, 1);
         launched("count_cta_kernel<256>", st);
         if (q.nmid_x + q.nmid_l) {

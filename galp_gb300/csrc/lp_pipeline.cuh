@@ -676,7 +676,7 @@ struct BlockRed5 {
 // One CTA of THREADS threads per vertex of degree <= SLOTS/2 (table of SLOTS 64-bit
 // slots in dynamic shared memory), for a range of the degree-sorted mid list.
 template <int THREADS, int SLOTS>
-__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 ? 2 : THREADS >= 256 ? 6 : 12)
+__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 ? 2 : THREADS >= 256 ? 5 : 10)
     count_cta_kernel(PipeArgs p, int which)
 {
     extern __shared__ __align__(16) unsigned long long cta_tab[];
