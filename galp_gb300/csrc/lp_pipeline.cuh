@@ -709,7 +709,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
         }
         const int64_t o0 = __ldg(&p.off[v]);
         const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
-        const uint32_t cap = 2 * pad32(deg);
+        // probe range: the whole table up to 4 slots per neighbour (load <= 1/4 where the
+        // table allows, at most 1/2): the longest probe of a warp's inserts sets its pace
+        const uint32_t cap = (uint32_t)min(SLOTS, 4 * pad32(deg));
         const bool agg = use_aggregation(p, v, deg);
         Sum5 obs = sum5_empty();
         // gather in rounds of PER loads per thread in flight together
