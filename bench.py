@@ -565,7 +565,7 @@ def run_gpu(args, g, desc, rank, world, dist):
         "data": "synthetic", "config": cfg, "clocks": clk.summary(), "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_val, 3) if e2e_val else None, "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_t, 4)},
+                "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_t, 4) if e2e_times else None},
         "dispatch": dispatch,
         "gpu_launches": int(launches_timed),
         "iteration_ms": round(ms_per_step / NITER, 4),
