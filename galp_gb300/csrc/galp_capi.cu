@@ -597,6 +597,15 @@ PipeArgs Engine::pipe_args(const Scope &sc) const
 }
 
 // One update of one scope: reads lab_in (all vertices), writes lab_out for the scope.
+int Engine::launch_limits()
+{
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_mid, count_mid64_kernel, 32 * kMidWarps, 0));
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_resolve, resolve_small_kernel, kTB, 0));
+    occ_mid = std::max(occ_mid, 1);
+    occ_resolve = std::max(occ_resolve, 1);
+    return GALP_OK;
+}
+
 int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
                           int32_t *lab_out, const uint8_t *dirty, int32_t *changed)
 {
@@ -605,6 +614,10 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
             GALP_CUDA(cudaMemsetAsync(b_gtab.p, 0, b_gtab.bytes, st));
             hub_gen = 1;
         }
+    }
+    if (!occ_mid) {
+        int rc = launch_limits();
+        if (rc) return rc;
     }
     IterArgs a = big_args(sc);
     a.nbr = nbr;
@@ -635,15 +648,17 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
     }
     if (prof.on) e0 = prof.mark(st);
     if (q.npacks) {
+        // several waves: blocks that finish early take up the remaining ones (pack costs vary)
         const int blocks = (int)std::min<int64_t>(((int64_t)q.npacks * 32 + 255) / 256, (int64_t)sms * small_bps);
         count_small_kernel<<<blocks, 256, 0, st>>>(q);
         launched("count_small_kernel", st);
     }
     if (q.nmid_s + q.nmid_l + q.nmid_x) {
         // ranges of the degree-sorted mid list come from the dispatch state
-        count_mid_kernel<<<(int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1, (int64_t)sms * mid_bps),
-                           32 * kMidWarps, 0, st>>>(q);
-        launched("count_mid_kernel", st);
+        count_mid64_kernel<<<(int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1,
+                                                    (int64_t)sms * std::min(mid_bps, occ_mid)),
+                             32 * kMidWarps, 0, st>>>(q);
+        launched("count_mid64_kernel", st);
         count_cta_kernel<128, 2 * kLargeAMax>
             <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 10)), 128,
                sizeof(unsigned long long) * 2 * kLargeAMax, st>>>(q, 0);
@@ -680,7 +695,7 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
                                                                 (const Ctl *)b_ctl.p, (int64_t *)b_g_base.p);
         launched("batch_bases_kernel", st);
     }
-    resolve_small_kernel<<<sms * resolve_bps, kTB, 0, st>>>(q);
+    resolve_small_kernel<<<sms * std::min(resolve_bps, occ_resolve), kTB, 0, st>>>(q);
     launched("resolve_small_kernel", st);
     if (q.nmid_s + q.nmid_l + q.nmid_x) {
         resolve_mid_kernel<<<sms * 2, kTB, 0, st>>>(q);

@@ -538,20 +538,23 @@ __device__ __forceinline__ void carry_clean(const PipeArgs &p, int v)
     else p.lab_out[v] = __ldg(&p.lab_in[v]);
 }
 
-// One warp per mid vertex (33..256 neighbours): a 512-slot table of 32-bit keys and
-// counts per warp, cleared per vertex (at warp scope plain 32-bit atomics beat the
-// generation-tagged slots).
-__global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
+// One warp per mid vertex (33..256 neighbours): a 512-slot table of generation-tagged
+// 64-bit slots per warp (as the CTA tables: never cleared between vertices), probed over
+// up to 4 slots per neighbour.  Against 32-bit key and count arrays cleared per vertex:
+// no clear pass and one shared-memory atomic per insert.
+__global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
 {
-    __shared__ uint32_t skey[kMidWarps][kMidSCap];
-    __shared__ uint32_t scnt[kMidWarps][kMidSCap];
+    __shared__ unsigned long long stab[kMidWarps][kMidSCap];
     if (!ctl_active(p.ctl)) return;
     const bool fr = frontier_on(p);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int gw = blockIdx.x * kMidWarps + w;
     const int nw = gridDim.x * kMidWarps;
     unsigned long long changes = 0;
-    uint32_t *key = skey[w], *cnt = scnt[w];
+    unsigned long long *tab = stab[w];
+    for (int s = lane; s < kMidSCap; s += 32) tab[s] = 0ull;
+    uint32_t gen = 0;
+    __syncwarp();
     const int nwarp_v = p.disp->pos1;  // the degree-sorted mid list's prefix of warp vertices
     for (int i = gw; i < nwarp_v; i += nw) {
         const int v = p.mid_v[i];
@@ -559,14 +562,14 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
             if (lane == 0) carry_clean(p, v);
             continue;
         }
+        if (++gen > kT64GenMax) {
+            for (int s = lane; s < kMidSCap; s += 32) tab[s] = 0ull;
+            __syncwarp();
+            gen = 1;
+        }
         const int64_t o0 = __ldg(&p.off[v]);
         const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
-        const int cap = 2 * pad32(deg);
-        for (int s = lane; s < cap; s += 32) {
-            key[s] = kEmpty;
-            cnt[s] = 0;
-        }
-        __syncwarp();
+        const uint32_t cap = (uint32_t)min(kMidSCap, 4 * pad32(deg));
         constexpr int PER = kMidSMax / 32;
         int nb[PER];
 #pragma unroll
@@ -582,46 +585,29 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid_kernel(PipeArgs p)
         for (int u = 0; u < PER; ++u) {
             if (u * 32 >= deg) break;  // warp-uniform
             // lanes holding the same label add once (heavy labels would serialise)
-            const unsigned same = __match_any_sync(kFull, lb[u]);
-            if (lb[u] == kEmpty || lane != __ffs(same) - 1) continue;
-            const uint32_t c = (uint32_t)__popc(same);
-            uint32_t h = hslot(lb[u], (uint32_t)cap);
-            for (;;) {
-                const uint32_t prev = atomicCAS(&key[h], kEmpty, lb[u]);
-                if (prev == kEmpty || prev == lb[u]) {
-                    part.d += prev == kEmpty;
-                    sum5_observe(part, (int)lb[u], (int)(atomicAdd(&cnt[h], c) + c));
-                    break;
-                }
-                h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
-            }
+            t64_insert_row(tab, cap, gen, lb[u], true, part);
         }
         __syncwarp();
         const Sum5 sm = sum5_warp(part);
         int rmin = 0, rmax = sm.d - 1;  // when every distinct label is a candidate
         if (sm.k > 1) {
             if (sm.k < sm.d) {
-                int a0 = 0, a1 = 0;
-                for (int s = lane; s < cap; s += 32)
-                    if (key[s] != kEmpty) {
-                        a0 += (int)key[s] < sm.mn;
-                        a1 += (int)key[s] < sm.mx;
-                    }
-                rmin = __reduce_add_sync(kFull, a0);
-                rmax = __reduce_add_sync(kFull, a1);
+                t64_ranks(tab, (int)cap, lane, 32, gen, sm.mn, sm.mx, rmin, rmax);
+                rmin = __reduce_add_sync(kFull, rmin);
+                rmax = __reduce_add_sync(kFull, rmax);
             }
             if (sm.k > 2) {  // resolving may need the runs themselves (unsorted)
                 int32_t *rl = p.run_lab + (o0 - p.nbr_shift);
                 uint16_t *rc = p.run_cnt + (o0 - p.nbr_shift);
                 int base = 0;
-                for (int s0 = 0; s0 < cap; s0 += 32) {
-                    const int s = s0 + lane;
-                    const bool occ = key[s] != kEmpty;  // cap is a multiple of 64
+                for (int s0 = 0; s0 < (int)cap; s0 += 32) {  // cap is a multiple of 128
+                    const unsigned long long x = tab[s0 + lane];
+                    const bool occ = (uint32_t)(x >> kT64GenShift) == gen;
                     const unsigned m = __ballot_sync(kFull, occ);
                     if (occ) {
                         const int at = base + __popc(m & ((1u << lane) - 1));
-                        rl[at] = (int32_t)key[s];
-                        rc[at] = (uint16_t)cnt[s];
+                        rl[at] = (int32_t)((x >> 14) & 0x7FFFFFFF);
+                        rc[at] = (uint16_t)(x & kT64CntMask);
                     }
                     base += __popc(m);
                 }
