@@ -943,8 +943,9 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
 {
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
-    __shared__ uint16_t sused[kBigChunk];  // occupied local slots, compacted
-    __shared__ int nused;
+    __shared__ uint16_t sused[kBigChunk];     // occupied local slots, compacted
+    __shared__ uint32_t screated[kBigChunk];  // global slots this chunk claimed
+    __shared__ int nused, ncreated, obase;
     if (!ctl_active(p.ctl)) return;
     if ((int)blockIdx.x >= p.nchunks) return;
     const int ch = p.c0 + blockIdx.x;
@@ -955,7 +956,7 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
         skey[s] = kEmpty;
         scnt[s] = 0;
     }
-    if (threadIdx.x == 0) nused = 0;
+    if (threadIdx.x == 0) nused = ncreated = 0;
     __syncthreads();
     {
         // all of a thread's neighbour loads, then all its label gathers, in flight together
@@ -968,7 +969,7 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
         }
         uint32_t lb[PER];
 #pragma unroll
-        for (int i = 0; i < PER; ++i) lb[i] = (nb[i] >= 0) ? (uint32_t)ld_label(&p.lab_in[nb[i]]) : kEmpty;
+        for (int i = 0; i < PER; ++i) lb[i] = (nb[i] >= 0) ? (uint32_t)__ldg(&p.lab_in[nb[i]]) : kEmpty;
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const uint32_t L = lb[i];
@@ -1094,16 +1095,23 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
                 }
             }
             if (created) observe(L[u], c[u]);
-            // record newly occupied slots in the vertex's occupied list (warp-aggregated)
+            // collect the claimed slots (warp-aggregated) for the vertex's occupied list
             const unsigned m = __ballot_sync(kFull, created);
             if (m) {
                 int ob = 0;
-                if (lane == __ffs(m) - 1) ob = atomicAdd(dcount, __popc(m));
+                if (lane == __ffs(m) - 1) ob = atomicAdd(&ncreated, __popc(m));
                 ob = __shfl_sync(kFull, ob, __ffs(m) - 1);
-                if (created) occ[ob + __popc(m & ((1u << lane) - 1))] = h[u];
+                if (created) screated[ob + __popc(m & ((1u << lane) - 1))] = h[u];
             }
         }
     }
+    // one reservation in the occupied list per chunk (the distinct count), then a
+    // coalesced copy: the chunks of one hub run together, so per-warp reservations
+    // would queue on the same counter
+    __syncthreads();
+    if (threadIdx.x == 0) obase = ncreated ? atomicAdd(dcount, ncreated) : 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < ncreated; i += kTB) occ[obase + i] = screated[i];
     // the chunk's partial summary -> bpart (the key arrays are no longer read: reuse)
     {
         const int Ww = __reduce_max_sync(kFull, oW);
