@@ -34,6 +34,7 @@ WORKLOADS = {
     # name: (kind, params)
     "rmat26": ("rmat", dict(scale=26, edge_factor=28)),
     "rmat24": ("rmat", dict(scale=24, edge_factor=16)),
+    "rmat23": ("rmat", dict(scale=23, edge_factor=16)),
     "rmat22": ("rmat", dict(scale=22, edge_factor=16)),
     "rmat20": ("rmat", dict(scale=20, edge_factor=16)),
     "lfr1m": ("lfr", dict(n=1_000_000)),
