@@ -973,12 +973,13 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
 #pragma unroll
         for (int i = 0; i < PER; ++i) {
             const uint32_t L = lb[i];
-            if (L == kEmpty) continue;
+            const unsigned same = __match_any_sync(kFull, L);
+            if (L == kEmpty || (int)(threadIdx.x & 31) != __ffs(same) - 1) continue;
             uint32_t h = hslot(L, cap);
             for (;;) {
                 uint32_t prev = atomicCAS(&skey[h], kEmpty, L);
                 if (prev == kEmpty || prev == L) {
-                    atomicAdd(&scnt[h], 1u);
+                    atomicAdd(&scnt[h], (uint32_t)__popc(same));
                     break;
                 }
                 h = (h + 1 == cap) ? 0 : h + 1;

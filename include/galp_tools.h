@@ -52,8 +52,8 @@ typedef struct {
 
 /* Kernel variant knobs.  Every variant computes the same labels; they differ in speed. */
 typedef struct {
-    int32_t agg_mode;      /* warp-aggregated table inserts: 0 auto (by last distinct count), 1 always,
-                              2 never (default) */
+    int32_t agg_mode;      /* warp-aggregated table inserts: 0 auto (by last distinct count, default),
+                              1 always, 2 never */
     float frontier_frac;   /* fixed rule, frontier mode: an iteration after more than this fraction
                               of labels changed recounts every vertex (default 0.05) */
     float learned_margin;  /* learned rule: predicted log gain needed to leave the fixed rule's
