@@ -58,6 +58,13 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
+// Four consecutive 64-bit slots (one 32-byte sector, p 32-byte aligned), two 16-byte
+// relaxed loads in flight together.
+__device__ __forceinline__ void ld_relaxed_group4(const unsigned long long *p, unsigned long long x[4])
+{
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(x[0]), "=l"(x[1]) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(x[2]), "=l"(x[3]) : "l"(p + 2) : "memory");
+}
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v)
 {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");

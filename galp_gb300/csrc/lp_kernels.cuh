@@ -341,6 +341,7 @@ struct RunListQuery {
 struct SplitTable {  // separate key and count arrays (shared-memory regions)
     const uint32_t *key;
     const uint32_t *cnt;
+    __device__ static uint32_t start(uint32_t k, uint32_t cap) { return hslot(k, cap); }
     __device__ uint32_t k(int s) const { return key[s]; }
     __device__ uint32_t c(int s) const { return cnt[s]; }
 };
@@ -348,6 +349,8 @@ struct HubTable {  // generation-tagged 64-bit slots (global hub tables)
     const unsigned long long *tab;
     int cbits, gshift;
     uint32_t lmask, gen;
+    // probing starts at the 4-slot (32-byte) group of the hash slot
+    __device__ static uint32_t start(uint32_t k, uint32_t cap) { return hslot(k, cap) & ~3u; }
     __device__ uint32_t k(int s) const
     {
         const unsigned long long x = tab[s];
@@ -464,7 +467,7 @@ struct WarpTableQueryT {
     }
     __device__ uint32_t count_of(uint32_t k) const
     {
-        uint32_t h = hslot(k, (uint32_t)cap);
+        uint32_t h = T::start(k, (uint32_t)cap);
         for (int probes = 0; probes < cap; ++probes) {
             const uint32_t x = t.k((int)h);
             if (x == k) return t.c((int)h);
@@ -1029,81 +1032,58 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
             omx = max(omx, (int)L);
         }
     };
-    constexpr int U = 2;  // slots per thread with their table reads in flight together
-    for (int base = 0; base < nloc; base += kTB * U) {  // block-uniform trip count
-        uint32_t L[U], h[U], ls[U];
-        unsigned long long cur[U];
+    // Probing walks 4-slot groups (one 32-byte sector, read with two 16-byte loads in
+    // flight together) from the group of the hash slot: the same slot order as linear
+    // probing from the group's first slot, with one memory round trip per group.
+    for (int base = 0; base < nloc; base += kTB) {  // block-uniform trip count
+        const int i = base + threadIdx.x;
+        bool created = false;
+        uint32_t g = 0, j = 0;
+        if (i < nloc) {
+            const uint32_t ls = sused[i], L = skey[ls], c = scnt[ls];
+            const unsigned long long tag = ((unsigned long long)gen << p.hub_gshift) |
+                                           ((unsigned long long)L << p.hub_cbits);
+            const unsigned long long key = tag >> p.hub_cbits;
+            g = hslot(L, gcap) & ~3u;
+            for (;;) {
+                unsigned long long x[4];
+                ld_relaxed_group4(&gt[g], x);
+                bool done = false;
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int i = base + u * kTB + threadIdx.x;
-            ls[u] = i < nloc ? sused[i] : 0u;
-            L[u] = i < nloc ? skey[ls[u]] : kEmpty;
-            h[u] = (L[u] != kEmpty) ? hslot(L[u], gcap) : 0;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) cur[u] = (L[u] != kEmpty) ? *(volatile unsigned long long *)&gt[h[u]] : 0ull;
-        // first attempt for all U slots together: add to a slot holding the label, or
-        // claim a free one (the claims' compare-and-swaps in flight together)
-        unsigned long long tag[U], prev[U];
-        uint32_t c[U];
-        int state[U];  // 0 nothing to do, 1 done, 2 claim issued, 3 probe on
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            state[u] = 0;
-            if (L[u] == kEmpty) continue;
-            c[u] = scnt[ls[u]];
-            tag[u] = ((unsigned long long)gen << p.hub_gshift) | ((unsigned long long)L[u] << p.hub_cbits);
-            if ((cur[u] >> p.hub_cbits) == (tag[u] >> p.hub_cbits)) {  // same generation and label
-                observe(L[u], (atomicAdd((unsigned int *)&gt[h[u]], c[u]) & cmask) + c[u]);
-                state[u] = 1;
-            } else {
-                state[u] = (uint32_t)(cur[u] >> p.hub_gshift) != gen ? 2 : 3;
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u)
-            if (state[u] == 2) prev[u] = atomicCAS(&gt[h[u]], cur[u], tag[u] | c[u]);
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            bool created = false;
-            if (state[u] == 2) {
-                if (prev[u] == cur[u]) {
-                    created = true;
-                    state[u] = 1;
-                } else {
-                    cur[u] = prev[u];
-                    state[u] = 3;
-                }
-            }
-            if (state[u] == 3) {  // the slot changed or belongs to another label
-                for (;;) {
-                    if ((cur[u] >> p.hub_cbits) == (tag[u] >> p.hub_cbits)) {
-                        observe(L[u], (atomicAdd((unsigned int *)&gt[h[u]], c[u]) & cmask) + c[u]);
-                        break;
-                    }
-                    if ((uint32_t)(cur[u] >> p.hub_gshift) != gen) {  // free: claim it
-                        const unsigned long long pv = atomicCAS(&gt[h[u]], cur[u], tag[u] | c[u]);
-                        if (pv == cur[u]) {
-                            created = true;
+                for (int jj = 0; jj < 4; ++jj) {
+                    if (done) break;
+                    unsigned long long xv = x[jj];
+                    for (;;) {
+                        if ((xv >> p.hub_cbits) == key) {  // same generation and label
+                            observe(L, (atomicAdd((unsigned int *)&gt[g + jj], c) & cmask) + c);
+                            done = true;
                             break;
                         }
-                        cur[u] = pv;
-                        continue;
+                        if ((uint32_t)(xv >> p.hub_gshift) != gen) {  // free: claim it
+                            const unsigned long long pv = atomicCAS(&gt[g + jj], xv, tag | c);
+                            if (pv == xv) {
+                                observe(L, c);
+                                created = done = true;
+                                break;
+                            }
+                            xv = pv;  // taken meanwhile: look at it again
+                            continue;
+                        }
+                        break;  // another label's slot: the next one
                     }
-                    // linear probing past slots owned by other labels (rare at load <= 1/2)
-                    h[u] = (h[u] + 1 == gcap) ? 0 : h[u] + 1;
-                    cur[u] = *(volatile unsigned long long *)&gt[h[u]];
+                    if (done) j = (uint32_t)jj;
                 }
+                if (done) break;
+                g = (g + 4 == gcap) ? 0 : g + 4;  // gcap is a multiple of 4
             }
-            if (created) observe(L[u], c[u]);
-            // collect the claimed slots (warp-aggregated) for the vertex's occupied list
-            const unsigned m = __ballot_sync(kFull, created);
-            if (m) {
-                int ob = 0;
-                if (lane == __ffs(m) - 1) ob = atomicAdd(&ncreated, __popc(m));
-                ob = __shfl_sync(kFull, ob, __ffs(m) - 1);
-                if (created) screated[ob + __popc(m & ((1u << lane) - 1))] = h[u];
-            }
+        }
+        // collect the claimed slots (warp-aggregated) for the vertex's occupied list
+        const unsigned m = __ballot_sync(kFull, created);
+        if (m) {
+            int ob = 0;
+            if (lane == __ffs(m) - 1) ob = atomicAdd(&ncreated, __popc(m));
+            ob = __shfl_sync(kFull, ob, __ffs(m) - 1);
+            if (created) screated[ob + __popc(m & ((1u << lane) - 1))] = g + j;
         }
     }
     // one reservation in the occupied list per chunk (the distinct count), then a
