@@ -170,8 +170,10 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             const int32_t b = (int32_t)S.big_v.size();
             S.big_v.push_back(v);
             S.big_c0.push_back((int32_t)S.chunk_big.size());
-            // load <= 1/2; a multiple of four slots keeps every table on 32-byte sectors
-            const uint32_t cap = (uint32_t)std::min<int64_t>((2 * deg + 3) & ~(int64_t)3, 0xFFFFFFFCll);
+            // 4 slots per edge (load <= 1/4: the probes, one memory round trip per 4-slot
+            // group, cost more than the larger footprint); a multiple of four slots keeps
+            // every table on 32-byte sectors
+            const uint32_t cap = (uint32_t)std::min<int64_t>(4 * deg, 0xFFFFFFFCll);
             S.big_toff.push_back(toff);
             S.big_tcap.push_back(cap);
             S.big_ooff.push_back(ooff);

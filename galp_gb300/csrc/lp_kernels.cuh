@@ -97,7 +97,7 @@ struct IterArgs {
     int32_t nbig;
     const int32_t *big_v;       // vertex of each big entry
     const int64_t *big_toff;    // table offset of each big entry
-    const uint32_t *big_tcap;   // table capacity (>= 2 * degree)
+    const uint32_t *big_tcap;   // table capacity (4 * degree, a multiple of 4)
     const int32_t *chunk_big;   // insert chunk -> big index
     const int64_t *chunk_e0;    // insert chunk -> first edge
     const int64_t *chunk_e1;    // insert chunk -> end edge
