@@ -603,8 +603,10 @@ int Engine::launch_limits()
 {
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_mid, count_mid64_kernel, 32 * kMidWarps, 0));
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_resolve, resolve_small_kernel, kTB, 0));
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_resolve_mid, resolve_mid_kernel, kTB, 0));
     occ_mid = std::max(occ_mid, 1);
     occ_resolve = std::max(occ_resolve, 1);
+    occ_resolve_mid = std::max(occ_resolve_mid, 1);
     return GALP_OK;
 }
 
@@ -700,7 +702,7 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
     resolve_small_kernel<<<sms * std::min(resolve_bps, occ_resolve), kTB, 0, st>>>(q);
     launched("resolve_small_kernel", st);
     if (q.nmid_s + q.nmid_l + q.nmid_x) {
-        resolve_mid_kernel<<<sms * 2, kTB, 0, st>>>(q);
+        resolve_mid_kernel<<<sms * occ_resolve_mid, kTB, 0, st>>>(q);
         launched("resolve_mid_kernel", st);
     }
     if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});

@@ -223,10 +223,10 @@ struct Engine {
     int64_t max_label = 0;    // labels stay below this (n, or the largest graph of a batch)
     // launch shapes (blocks per SM), chosen by galp_batch_tune
     int small_bps = 16, mid_bps = 6, resolve_bps = 4;
-    // resident blocks per SM of the mid-vertex counting and small-vertex resolve kernels
-    // (occupancy API): their grid-stride loops run as one wave, since a partial second
-    // wave would start its blocks' whole shares late
-    int occ_mid = 0, occ_resolve = 0;
+    // resident blocks per SM of the mid-vertex counting and the resolve kernels (occupancy
+    // API): their grid-stride loops run as one full wave, since a partial second wave
+    // would start its blocks' whole shares late
+    int occ_mid = 0, occ_resolve = 0, occ_resolve_mid = 0;
     int launch_limits();
     int setup_batch(const galp_csr &g, const int64_t *graph_v0, int32_t count, const galp_opts &o, cudaStream_t st,
                     int64_t &h2d);
