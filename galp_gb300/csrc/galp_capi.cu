@@ -272,26 +272,29 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     h_nbr = g.neighbors;
     frontier = o.frontier != 0 && policy == 0;  // the frontier needs the whole graph resident
     max_label = n;
-    std::vector<int64_t> starts;
-    if (policy == 0) {
-        starts = {0, n};
-    } else {
-        if (o.buffer_pow < 1 || o.buffer_pow > 40) return GALP_EINVAL;
-        int rc = batch_boundaries(n, g.offsets, o.buffer_pow, starts);
-        if (rc) return rc;
-    }
-    if (!build_schedule(sched, n, g.offsets, starts)) return GALP_EFORMAT;
-    phase(0);
-
+    if (policy != 0 && (o.buffer_pow < 1 || o.buffer_pow > 40)) return GALP_EINVAL;
     GALP_CUDA(b_off.alloc(sizeof(int64_t) * (n + 1)));
+    if (policy == 0) GALP_CUDA(b_nbr[0].alloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
+    // the CSR upload runs while the host builds the schedule (host or device neighbours:
+    // batched callers may hand over a device array)
     GALP_CUDA(cudaMemcpyAsync(b_off.p, g.offsets, sizeof(int64_t) * (n + 1), cudaMemcpyDefault, st));
     h2d += sizeof(int64_t) * (n + 1);
-    if (policy == 0) {
-        GALP_CUDA(b_nbr[0].alloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
-        // host or device neighbours (batched callers may hand over a device array)
-        if (m) GALP_CUDA(cudaMemcpyAsync(b_nbr[0].p, g.neighbors, sizeof(int32_t) * m, cudaMemcpyDefault, st));
+    if (policy == 0 && m) {
+        GALP_CUDA(cudaMemcpyAsync(b_nbr[0].p, g.neighbors, sizeof(int32_t) * m, cudaMemcpyDefault, st));
         h2d += sizeof(int32_t) * m;
-    } else {
+    }
+    std::vector<int64_t> starts;
+    int brc = GALP_OK;
+    if (policy == 0) starts = {0, n};
+    else brc = batch_boundaries(n, g.offsets, o.buffer_pow, starts);
+    const bool sched_ok = brc == GALP_OK && build_schedule(sched, n, g.offsets, starts);
+    if (!sched_ok) {
+        GALP_CUDA(cudaStreamSynchronize(st));  // the copies read the caller's buffers
+        return brc != GALP_OK ? brc : GALP_EFORMAT;
+    }
+    phase(0);
+
+    if (policy != 0) {
         const size_t cap = sizeof(int32_t) * std::max<int64_t>(sched.max_scope_edges, 1);
         GALP_CUDA(b_nbr[0].alloc(cap));
         GALP_CUDA(b_nbr[1].alloc(cap));
