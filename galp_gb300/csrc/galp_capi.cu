@@ -104,6 +104,32 @@ void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
 
 }  // namespace
 
+// Hub table capacity: `per_edge` slots per edge, a multiple of four slots (tables stay on
+// 32-byte sectors).  Four per edge (load <= 1/4) is the default: the probes, one memory
+// round trip per 4-slot group, cost more than the larger footprint.
+constexpr int kHubSlotsPerEdge = 4;
+uint32_t hub_table_slots(int64_t deg, int per_edge)
+{
+    return (uint32_t)std::min<int64_t>((per_edge * deg + 3) & ~(int64_t)3, 0xFFFFFFFCll);
+}
+
+// Re-size every hub table at `per_edge` slots per edge (table offsets, per-scope sizes).
+void resize_hub_tables(Schedule &S, const int64_t *off, int per_edge)
+{
+    S.max_table_slots = 0;
+    for (Scope &sc : S.scopes) {
+        int64_t toff = 0;
+        for (int32_t b = sc.b0; b < sc.b0 + sc.nb; ++b) {
+            const int32_t v = S.big_v[(size_t)b];
+            S.big_toff[(size_t)b] = toff;
+            S.big_tcap[(size_t)b] = hub_table_slots(off[v + 1] - off[v], per_edge);
+            toff += S.big_tcap[(size_t)b];
+        }
+        sc.table_slots = toff;
+        S.max_table_slots = std::max(S.max_table_slots, toff);
+    }
+}
+
 // Static per-graph schedule (host), per scope: packs of consecutive vertices of degree
 // <= 32 (at most 32 vertices and 32 edges; a pack ends at a vertex of another bucket or
 // at a thread's chunk boundary), the mid list (33..12288) in ascending degree, and big
@@ -170,10 +196,7 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             const int32_t b = (int32_t)S.big_v.size();
             S.big_v.push_back(v);
             S.big_c0.push_back((int32_t)S.chunk_big.size());
-            // 4 slots per edge (load <= 1/4: the probes, one memory round trip per 4-slot
-            // group, cost more than the larger footprint); a multiple of four slots keeps
-            // every table on 32-byte sectors
-            const uint32_t cap = (uint32_t)std::min<int64_t>(4 * deg, 0xFFFFFFFCll);
+            const uint32_t cap = hub_table_slots(deg, kHubSlotsPerEdge);
             S.big_toff.push_back(toff);
             S.big_tcap.push_back(cap);
             S.big_ooff.push_back(ooff);
@@ -291,6 +314,14 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     if (!sched_ok) {
         GALP_CUDA(cudaStreamSynchronize(st));  // the copies read the caller's buffers
         return brc != GALP_OK ? brc : GALP_EFORMAT;
+    }
+    {
+        // hub tables at 2 slots per edge when 4 would take more than a third of the free
+        // device memory (very hub-heavy graphs)
+        size_t free_b = 0, total_b = 0;
+        GALP_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        if ((double)sizeof(unsigned long long) * (double)sched.max_table_slots > (double)free_b / 3)
+            resize_hub_tables(sched, g.offsets, 2);
     }
     phase(0);
 

@@ -66,7 +66,7 @@ struct Schedule {
     std::vector<int32_t> mid_deg;    // degree of each mid_v entry
     std::vector<int32_t> big_v;      // vertex of each big entry
     std::vector<int64_t> big_toff;   // table offset, relative to its scope
-    std::vector<uint32_t> big_tcap;  // table capacity (4 * degree)
+    std::vector<uint32_t> big_tcap;  // table capacity (4 slots per edge; 2 when device memory is short)
     std::vector<int64_t> big_ooff;   // occupied-list offset, relative to its scope
     std::vector<int32_t> chunk_big;
     std::vector<int64_t> chunk_e0, chunk_e1;

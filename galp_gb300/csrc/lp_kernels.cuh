@@ -13,8 +13,8 @@
 // decoupled look-back over the preceding tiles, and resolve every vertex's winner
 // with the positional tie rule while the tile is still on chip.  Vertices of degree
 // above kTileSlots ("big") are counted beforehand into global hash tables by
-// big_insert/big_combine (big_stats adds candidate ranks), take part in the scan as single-vertex tiles, and are
-// resolved by big_resolve once their run base is known.
+// big_insert and big_combine (big_stats adds candidate ranks), take part in the scan
+// as single-vertex tiles, and are resolved by big_resolve once their run base is known.
 //
 // Reference counterparts: DPPBase::perform_lp (label_propagation/src/dpp/dpp.cuh:104-138),
 // gather_labels..update_labels (src/dpp/kernel.cuh:27-119), the segmented sort and
@@ -34,7 +34,7 @@ constexpr int kTileSlots = 2048;      // shared-memory label slots per tile
 constexpr int kTileV = 512;           // vertices per tile
 constexpr int kSmallMax = 32;         // degree handled by one warp pack
 constexpr int kBigChunk = 1024;       // edges per big_insert CTA
-constexpr int kBigSlotChunk = 8192;   // table slots per big_stats CTA
+constexpr int kBigSlotChunk = 8192;   // occupied-list entries per big_stats CTA
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
 constexpr long long kSpinLimit = 1ll << 20;  // look-back give-up bound (about a second)
@@ -97,7 +97,7 @@ struct IterArgs {
     int32_t nbig;
     const int32_t *big_v;       // vertex of each big entry
     const int64_t *big_toff;    // table offset of each big entry
-    const uint32_t *big_tcap;   // table capacity (4 * degree, a multiple of 4)
+    const uint32_t *big_tcap;   // table capacity (4 or 2 slots per edge, a multiple of 4)
     const int32_t *chunk_big;   // insert chunk -> big index
     const int64_t *chunk_e0;    // insert chunk -> first edge
     const int64_t *chunk_e1;    // insert chunk -> end edge
