@@ -42,7 +42,7 @@ def _load():
         P = ctypes.c_void_p
         L.oracle_run.restype = ctypes.c_int64
         L.oracle_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                                 ctypes.c_int, ctypes.c_int, P, P]
+                                 ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P]
         L.oracle_seg_reduce_check.restype = ctypes.c_int
         L.oracle_seg_reduce_check.argtypes = [P, ctypes.c_int64, P, ctypes.c_int64, ctypes.c_int, ctypes.c_int, P, P]
         L.oracle_batch_boundaries.restype = ctypes.c_int64
@@ -62,27 +62,11 @@ def run(offsets, neighbors, niter: int, policy: int = 0, buffer_pow: int = 24, l
     n = len(off) - 1
     lab = np.zeros(max(n, 1), np.int32)
     cnt = np.zeros(max(niter, 1), np.int64)
-    if early_exit:
-        it = L.oracle_run(n, off.ctypes.data, nbr.ctypes.data, niter, policy, buffer_pow, int(literal), TB, ET,
-                          lab.ctypes.data, cnt.ctypes.data)
-        if it < 0:
-            raise RuntimeError(f"oracle_run failed ({it})")
-        return int(it), lab[:n].copy(), cnt[:it].copy()
-    # no early exit: one iteration at a time
-    lab_all = None
-    counts = []
-    cur = None
-    for k in range(1, niter + 1):
-        it = L.oracle_run(n, off.ctypes.data, nbr.ctypes.data, k, policy, buffer_pow, int(literal), TB, ET,
-                          lab.ctypes.data, cnt.ctypes.data)
-        if it < 0:
-            raise RuntimeError(f"oracle_run failed ({it})")
-        if it < k:  # the early exit fired inside; continue from these labels is not expressible here
-            raise RuntimeError("oracle: early exit fired; use early_exit=True")
-        counts.append(int(cnt[k - 1]))
-        cur = lab[:n].copy()
-    lab_all = cur
-    return niter, lab_all, np.array(counts, np.int64)
+    it = L.oracle_run(n, off.ctypes.data, nbr.ctypes.data, niter, policy, buffer_pow, int(literal), TB, ET,
+                      int(bool(early_exit)), lab.ctypes.data, cnt.ctypes.data)
+    if it < 0:
+        raise RuntimeError(f"oracle_run failed ({it})")
+    return int(it), lab[:n].copy(), cnt[:it].copy()
 
 
 def seg_reduce_check(weights, seg_start, TB: int, ET: int):

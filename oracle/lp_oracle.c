@@ -604,10 +604,11 @@ int64_t oracle_batch_boundaries(int64_t n, const int64_t *offsets, int buffer_po
  * same labels).  labels_out[n] receives the final labels, counts_out[niter] the
  * per-iteration change counts.  literal != 0 selects the literal reduction
  * (TB/ET as given), else the closed form.  Returns the number of iterations run
- * (the loop breaks once count <= n * 1e-5), or a negative error.
+ * (with early_exit, the loop breaks once count <= n * 1e-5, dpp.cuh:88; without it,
+ * all niter iterations run), or a negative error.
  */
 int64_t oracle_run(int64_t n, const int64_t *offsets, const int32_t *neighbors, int niter,
-                   int policy, int buffer_pow, int literal, int TB, int ET,
+                   int policy, int buffer_pow, int literal, int TB, int ET, int early_exit,
                    int32_t *labels_out, int64_t *counts_out)
 {
     for (int64_t i = 0; i < n; ++i) labels_out[i] = (int32_t)i;
@@ -643,7 +644,7 @@ int64_t oracle_run(int64_t n, const int64_t *offsets, const int32_t *neighbors, 
             }
         }
         counts_out[it] = count;
-        if ((double)count <= (double)n * 1e-5) { ++it; break; }
+        if (early_exit && (double)count <= (double)n * 1e-5) { ++it; break; }
     }
     free(bbs);
     free(loff);
