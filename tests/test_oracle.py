@@ -143,3 +143,15 @@ def test_degree_zero_vertices_equal_compacted_graph():
     it, lab, cnt = oracle.run(g.offsets, g.neighbors, 10)
     assert np.array_equal(keep[lab], lab2[keep])
     assert (lab2[iso] == iso).all()
+
+
+def test_fixed_iteration_count_runs_past_convergence():
+    # early exit off: all iterations run (zero changes once converged) and the labels are
+    # those of the early-exit run; the first iterations' counts agree
+    g = galp_gb300.generate_sbm([64] * 8, 10.0, 0.5, seed=4)
+    it_e, lab_e, cnt_e = oracle.run(g.offsets, g.neighbors, 30)
+    it_f, lab_f, cnt_f = oracle.run(g.offsets, g.neighbors, 30, early_exit=False)
+    assert it_e < 30 and it_f == 30 and len(cnt_f) == 30
+    assert np.array_equal(lab_e, lab_f)
+    assert list(cnt_f[:it_e]) == list(cnt_e)
+    assert (cnt_f[it_e:] <= cnt_e[-1]).all()
