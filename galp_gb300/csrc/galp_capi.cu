@@ -59,6 +59,8 @@ struct ChunkPlan {
     std::vector<int32_t> pack_v0;
     std::vector<uint8_t> pack_nv;
     std::vector<int32_t> mid;
+    std::vector<int32_t> mid_deg;    // degree of each mid entry
+    std::vector<int64_t> mid_count;  // mid entries by degree (kXlMax + 1 bins), then positions
     std::vector<int32_t> big;
     int64_t nsmall = 0;
     int32_t last_v = -1;
@@ -68,6 +70,7 @@ struct ChunkPlan {
 
 void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
 {
+    P.mid_count.assign(kXlMax + 1, 0);
     int pv = 0, pe = 0;  // vertices / edges in the open pack
     int64_t pstart = -1;
     auto close = [&]() {
@@ -96,8 +99,13 @@ void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
             continue;
         }
         close();
-        if (deg <= kXlMax) P.mid.push_back((int32_t)v);
-        else P.big.push_back((int32_t)v);
+        if (deg <= kXlMax) {
+            P.mid.push_back((int32_t)v);
+            P.mid_deg.push_back((int32_t)deg);
+            ++P.mid_count[(size_t)deg];
+        } else {
+            P.big.push_back((int32_t)v);
+        }
     }
     close();
 }
@@ -164,31 +172,58 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             for (auto &x : th) x.join();
         }
         int64_t nsmall = 0;
-        std::vector<int32_t> mid, big;
+        std::vector<int32_t> big;
+        size_t np = 0, nm = 0;
         for (ChunkPlan &P : plans) {
             if (P.bad) return false;
-            S.pack_v0.insert(S.pack_v0.end(), P.pack_v0.begin(), P.pack_v0.end());
-            S.pack_nv.insert(S.pack_nv.end(), P.pack_nv.begin(), P.pack_nv.end());
-            mid.insert(mid.end(), P.mid.begin(), P.mid.end());
+            np += P.pack_v0.size();
+            nm += P.mid.size();
             big.insert(big.end(), P.big.begin(), P.big.end());
             nsmall += P.nsmall;
             if (P.last_v >= 0) sc.last_v = P.last_v;
             for (int b = 0; b < kDegBins; ++b) S.deg_hist[b] += P.hist[b];
         }
-        // the mid list in ascending degree (counting sort, stable): any degree threshold
-        // is a cut position, so the kernel split can change per iteration
+        // The mid list in ascending degree (counting sort, stable: threads in vertex order,
+        // each thread's entries in vertex order), so any degree threshold is a cut position
+        // and the kernel split can change per iteration.  Each thread's bins become its
+        // write positions; packs are copied to their offsets by the same threads.
+        const size_t pb = S.pack_v0.size(), mb = S.mid_v.size();
         {
-            std::vector<int64_t> at(kXlMax + 2, 0);
-            for (int32_t x : mid) ++at[(size_t)(off[x + 1] - off[x]) + 1];
-            for (size_t d = 1; d < at.size(); ++d) at[d] += at[d - 1];
-            sc.nms = (int32_t)at[kMidSMax + 1];
-            sc.nml = (int32_t)(at[kLargeMax + 1] - at[kMidSMax + 1]);
-            sc.nmx = (int32_t)(at[kXlMax + 1] - at[kLargeMax + 1]);
-            const size_t b = S.mid_v.size();
-            S.mid_v.resize(b + mid.size());
-            for (int32_t x : mid) S.mid_v[b + (size_t)at[(size_t)(off[x + 1] - off[x])]++] = x;
-            S.mid_deg.resize(S.mid_v.size());
-            for (size_t i = b; i < S.mid_v.size(); ++i) S.mid_deg[i] = (int32_t)(off[S.mid_v[i] + 1] - off[S.mid_v[i]]);
+            int64_t pos = (int64_t)mb;
+            for (int d = 0; d <= kXlMax; ++d) {
+                if (d == kMidSMax + 1) sc.nms = (int32_t)(pos - (int64_t)mb);
+                if (d == kLargeMax + 1) sc.nml = (int32_t)(pos - (int64_t)mb) - sc.nms;
+                for (ChunkPlan &P : plans) {
+                    const int64_t c = P.mid_count[(size_t)d];
+                    P.mid_count[(size_t)d] = pos;
+                    pos += c;
+                }
+            }
+            sc.nmx = (int32_t)(pos - (int64_t)mb) - sc.nms - sc.nml;
+        }
+        S.pack_v0.resize(pb + np);
+        S.pack_nv.resize(pb + np);
+        S.mid_v.resize(mb + nm);
+        S.mid_deg.resize(mb + nm);
+        {
+            auto place = [&](int t, size_t p0) {
+                ChunkPlan &P = plans[(size_t)t];
+                std::copy(P.pack_v0.begin(), P.pack_v0.end(), S.pack_v0.begin() + (ptrdiff_t)p0);
+                std::copy(P.pack_nv.begin(), P.pack_nv.end(), S.pack_nv.begin() + (ptrdiff_t)p0);
+                for (size_t i = 0; i < P.mid.size(); ++i) {
+                    const size_t at = (size_t)P.mid_count[(size_t)P.mid_deg[i]]++;
+                    S.mid_v[at] = P.mid[i];
+                    S.mid_deg[at] = P.mid_deg[i];
+                }
+            };
+            std::vector<std::thread> th;
+            size_t p0 = pb;
+            for (int t = 0; t < T; ++t) {
+                if (T == 1) place(t, p0);
+                else th.emplace_back(place, t, p0);
+                p0 += plans[(size_t)t].pack_v0.size();
+            }
+            for (auto &x : th) x.join();
         }
         int64_t toff = 0, ooff = 0;
         for (int32_t v : big) {
