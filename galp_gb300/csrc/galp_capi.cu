@@ -60,7 +60,7 @@ struct ChunkPlan {
     std::vector<uint8_t> pack_nv;
     std::vector<int32_t> mid;
     std::vector<int32_t> mid_deg;    // degree of each mid entry
-    std::vector<int64_t> mid_count;  // mid entries by degree (kXlMax + 1 bins), then positions
+    std::vector<int64_t> mid_count;  // mid entries by degree (up to the largest), then positions
     std::vector<int32_t> big;
     int64_t nsmall = 0;
     int32_t last_v = -1;
@@ -70,7 +70,6 @@ struct ChunkPlan {
 
 void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
 {
-    P.mid_count.assign(kXlMax + 1, 0);
     int pv = 0, pe = 0;  // vertices / edges in the open pack
     int64_t pstart = -1;
     auto close = [&]() {
@@ -102,6 +101,7 @@ void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
         if (deg <= kXlMax) {
             P.mid.push_back((int32_t)v);
             P.mid_deg.push_back((int32_t)deg);
+            if ((size_t)deg >= P.mid_count.size()) P.mid_count.resize((size_t)deg + 1, 0);
             ++P.mid_count[(size_t)deg];
         } else {
             P.big.push_back((int32_t)v);
@@ -189,17 +189,25 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         // write positions; packs are copied to their offsets by the same threads.
         const size_t pb = S.pack_v0.size(), mb = S.mid_v.size();
         {
-            int64_t pos = (int64_t)mb;
-            for (int d = 0; d <= kXlMax; ++d) {
-                if (d == kMidSMax + 1) sc.nms = (int32_t)(pos - (int64_t)mb);
-                if (d == kLargeMax + 1) sc.nml = (int32_t)(pos - (int64_t)mb) - sc.nms;
+            size_t D = 0;
+            for (const ChunkPlan &P : plans) D = std::max(D, P.mid_count.size());
+            int64_t pos = (int64_t)mb, upto_mid = -1, upto_large = -1;
+            for (size_t d = 0; d < D; ++d) {
+                if (d == (size_t)kMidSMax + 1) upto_mid = pos - (int64_t)mb;
+                if (d == (size_t)kLargeMax + 1) upto_large = pos - (int64_t)mb;
                 for (ChunkPlan &P : plans) {
-                    const int64_t c = P.mid_count[(size_t)d];
-                    P.mid_count[(size_t)d] = pos;
+                    if (d >= P.mid_count.size()) continue;
+                    const int64_t c = P.mid_count[d];
+                    P.mid_count[d] = pos;
                     pos += c;
                 }
             }
-            sc.nmx = (int32_t)(pos - (int64_t)mb) - sc.nms - sc.nml;
+            const int64_t total = pos - (int64_t)mb;
+            if (upto_mid < 0) upto_mid = total;
+            if (upto_large < 0) upto_large = total;
+            sc.nms = (int32_t)upto_mid;
+            sc.nml = (int32_t)(upto_large - upto_mid);
+            sc.nmx = (int32_t)(total - upto_large);
         }
         S.pack_v0.resize(pb + np);
         S.pack_nv.resize(pb + np);
