@@ -91,9 +91,15 @@ def build(force: bool = False, verbose: bool = False) -> None:
                               ["g++", "-O2", "-std=c++17", "-fopenmp", "-o", cli_out, cli_src, *host_srcs,
                                "-L" + LIB, "-lgalp", "-Wl,-rpath,$ORIGIN"]))
 
+    # oracle: the sequential restatement (C) and its multi-threaded closed form (C++/OpenMP)
+    # in one library
     orc_out = os.path.join(ORACLE, "_build", "liblp_oracle.so")
-    orc_src = [os.path.join(ORACLE, "lp_oracle.c")]
-    jobs.append((orc_out, orc_src, ["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-o", orc_out, *orc_src]))
+    orc_c = os.path.join(ORACLE, "lp_oracle.c")
+    orc_o = os.path.join(ORACLE, "_build", "lp_oracle.o")
+    orc_par = os.path.join(ORACLE, "lp_oracle_par.cpp")
+    jobs.append((orc_o, [orc_c], ["gcc", "-O2", "-std=c99", "-fPIC", "-c", "-o", orc_o, orc_c]))
+    link_jobs.append((orc_out, [orc_o, orc_par], ["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
+                                                  "-o", orc_out, orc_par, orc_o]))
     port_src = os.path.join(ORACLE, "cpu_worker_port.cpp")
     if os.path.exists(port_src):
         port_out = os.path.join(ORACLE, "_build", "libcpu_worker_port.so")

@@ -8,6 +8,7 @@ Contents
   lp_oracle.c          literal restatement of DPPBase::perform_lp and the segmented
                        arg-max (reference: src/dpp/dpp.cuh, src/dpp/kernel.cuh,
                        src/common/segmented_reduce.cuh) + the closed form of its tie rule
+  lp_oracle_par.cpp    the closed form, multi-threaded, for billion-entry graphs
   cpu_worker_port.cpp  port of the reference's CPU label update CPUWorker::update_label
                        (src/common/hybrid_cpu_worker.cuh:172-195), the timed CPU baseline
   refsim/              the reference's own kernels executed on the CPU (oracle/_ref/)
@@ -49,6 +50,14 @@ def _load():
         L.oracle_batch_boundaries.argtypes = [ctypes.c_int64, P, ctypes.c_int, P, ctypes.c_int64]
         L.oracle_cf_winner.restype = ctypes.c_int64
         L.oracle_cf_winner.argtypes = [P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int]
+        L.oracle_step_par.restype = ctypes.c_int64
+        L.oracle_step_par.argtypes = [ctypes.c_int64, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      P, ctypes.c_int]
+        L.oracle_run_par.restype = ctypes.c_int64
+        L.oracle_run_par.argtypes = [ctypes.c_int64, P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, ctypes.c_int]
+        L.oracle_par_threads.restype = ctypes.c_int
+        L.oracle_par_threads.argtypes = []
         _lib = L
     return _lib
 
@@ -67,6 +76,46 @@ def run(offsets, neighbors, niter: int, policy: int = 0, buffer_pow: int = 24, l
     if it < 0:
         raise RuntimeError(f"oracle_run failed ({it})")
     return int(it), lab[:n].copy(), cnt[:it].copy()
+
+
+def run_par(offsets, neighbors, niter: int, policy: int = 0, buffer_pow: int = 24, early_exit: bool = True,
+            labels=None, threads: int = 0, TB: int = 256, ET: int = 17):
+    """Multi-threaded closed form (lp_oracle_par.cpp), same results as run(): labels after
+    up to niter iterations starting from vertex IDs, or from `labels` when given.
+    Returns (iters_run, labels int32[n], counts int64[iters])."""
+    L = _load()
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    nbr = np.ascontiguousarray(neighbors, dtype=np.int32)
+    n = len(off) - 1
+    lab = np.zeros(max(n, 1), np.int32)
+    if labels is not None:
+        lab[:n] = np.asarray(labels, np.int32)
+    cnt = np.zeros(max(niter, 1), np.int64)
+    it = L.oracle_run_par(n, off.ctypes.data, nbr.ctypes.data if len(nbr) else None, niter, policy, buffer_pow, TB,
+                          ET, int(bool(early_exit)), int(labels is None), lab.ctypes.data, cnt.ctypes.data, threads)
+    if it < 0:
+        raise RuntimeError(f"oracle_run_par failed ({it})")
+    return int(it), lab[:n].copy(), cnt[:it].copy()
+
+
+def step_par(offsets, neighbors, labels, policy: int = 0, buffer_pow: int = 24, threads: int = 0,
+             TB: int = 256, ET: int = 17):
+    """One iteration from the given labels (multi-threaded closed form).
+    Returns (new labels int32[n], change count)."""
+    L = _load()
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    nbr = np.ascontiguousarray(neighbors, dtype=np.int32)
+    n = len(off) - 1
+    lab = np.array(labels, dtype=np.int32, copy=True)
+    c = L.oracle_step_par(n, off.ctypes.data, nbr.ctypes.data if len(nbr) else None, policy, buffer_pow, TB, ET,
+                          lab.ctypes.data if n else None, threads)
+    if c < 0:
+        raise RuntimeError(f"oracle_step_par failed ({c})")
+    return lab, int(c)
+
+
+def par_threads() -> int:
+    return int(_load().oracle_par_threads())
 
 
 def seg_reduce_check(weights, seg_start, TB: int, ET: int):

@@ -396,11 +396,20 @@ out:
 /* Closed form of the tie-break                                            */
 /* ---------------------------------------------------------------------- */
 
-static wx_t lmax_range(const int32_t *w, int64_t lo, int64_t hi)
+/* Run weights of a segment, addressed by global run index: at(i) = p[i - base].
+ * Only indexes inside the segment being resolved are ever read. */
+typedef struct {
+    const int32_t *p;
+    int64_t base;
+} wseg_t;
+
+static inline int32_t wat(wseg_t w, int64_t i) { return w.p[i - w.base]; }
+
+static wx_t lmax_range(wseg_t w, int64_t lo, int64_t hi)
 {
     wx_t r = WX_ID;
     for (int64_t i = lo; i < hi; ++i)
-        if (w[i] > r.w) { r.w = w[i]; r.x = i; }
+        if (wat(w, i) > r.w) { r.w = wat(w, i); r.x = i; }
     return r;
 }
 
@@ -420,17 +429,18 @@ static int64_t bitrev(int64_t t, int TB)
     return r;
 }
 
-static wx_t tree_pick(const int32_t *w, int64_t lo, int TB, int ET)
+static wx_t tree_pick(wseg_t w, int64_t lo, int TB, int ET)
 {
     wx_t r = WX_ID;
     int64_t best_key = -1;
     const int64_t E = (int64_t)TB * ET;
     for (int64_t i = 0; i < E; ++i) {
-        if (w[lo + i] > r.w) {
-            r.w = w[lo + i];
+        const int32_t x = wat(w, lo + i);
+        if (x > r.w) {
+            r.w = x;
             best_key = -1;
         }
-        if (w[lo + i] == r.w) {
+        if (x == r.w) {
             int64_t key = bitrev(i / ET, TB) * ET + (i % ET);
             if (key > best_key) {
                 best_key = key;
@@ -447,14 +457,14 @@ static inline int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
 /* contribution of an earlier tile j of segment [a, ...): the trailing-partial
  * carry (leftmost max) when the segment starts inside tile j, otherwise the
  * whole-tile tree reduction (tree_pick). */
-static wx_t tile_contrib(const int32_t *w, int64_t a, int64_t j, int TB, int ET)
+static wx_t tile_contrib(wseg_t w, int64_t a, int64_t j, int TB, int ET)
 {
     const int64_t E = (int64_t)TB * ET;
     if (a > j * E) return lmax_range(w, a, (j + 1) * E);
     return tree_pick(w, j * E, TB, ET);
 }
 
-static wx_t tiles_fold_L(const int32_t *w, int64_t a, int64_t j0, int64_t j1, int TB, int ET)
+static wx_t tiles_fold_L(wseg_t w, int64_t a, int64_t j0, int64_t j1, int TB, int ET)
 {
     wx_t acc = WX_ID;
     for (int64_t j = j0; j < j1; ++j) acc = opL(acc, tile_contrib(w, a, j, TB, ET));
@@ -462,13 +472,15 @@ static wx_t tiles_fold_L(const int32_t *w, int64_t a, int64_t j0, int64_t j1, in
 }
 
 /*
- * Winning run index of the segment [a, b) (run weights w[], global run index),
- * in a scope of N runs, for a reduction with TB threads x ET elements per tile.
+ * Winning run index of the segment [a, b) in a scope of N runs, for a reduction
+ * with TB threads x ET elements per tile; w_seg[i] is the weight of run a + i.
  * Derived from segmented_reduce.cuh; chunk = ET runs, tile = TB*ET runs,
- * spine block = TB tiles, level-2 chunk = TB spine blocks.  TB must be a power of two.
+ * spine block = TB tiles, level-2 chunk = TB spine blocks.  TB must be a power
+ * of two.  Every run index it reads lies in [a, b).
  */
-int64_t oracle_cf_winner(const int32_t *w, int64_t a, int64_t b, int64_t N, int TB, int ET)
+int64_t oracle_cf_winner_seg(const int32_t *w_seg, int64_t a, int64_t b, int64_t N, int TB, int ET)
 {
+    const wseg_t w = {w_seg, a};
     const int64_t C = ET, E = (int64_t)TB * ET, SB = TB, Q = TB;
     const int64_t e = (b == N) ? ((N + E - 1) / E) * E - 1 : b - 1;
     const int64_t ke = e / E, ce = e / C, sb = ke / SB, qe = sb / Q;
@@ -494,6 +506,12 @@ int64_t oracle_cf_winner(const int32_t *w, int64_t a, int64_t b, int64_t N, int 
         s = opL(acc, s_in);
     }
     return opR(s, d1).x;
+}
+
+/* The same over a scope-wide weight array w[N]. */
+int64_t oracle_cf_winner(const int32_t *w, int64_t a, int64_t b, int64_t N, int TB, int ET)
+{
+    return oracle_cf_winner_seg(w + a, a, b, N, TB, ET);
 }
 
 /*

@@ -2,13 +2,9 @@
 
 * LFR-style n = 1 M (the LFR configuration, methods 0 and 1): labels, iteration count and
   change counts equal the oracle after 10 iterations.
-* R-MAT scale 22 (2.4 M vertices, 128 M CSR entries): labels and change counts equal the
-  oracle after each of the first four iterations.
-* R-MAT scale 24 (8.9 M vertices, 521 M CSR entries, the R-MAT 24 configuration): the
-  full oracle is too slow for a test run, so size-independent properties are checked on a
-  seeded sample of 200,000 vertices for three consecutive iterations: the new label is a
-  label of maximum count among the vertex's neighbours' previous labels, and equals it
-  exactly where that maximum is unique; vertices without neighbours keep their label.
+* R-MAT scale 22 (2.4 M vertices, 128 M CSR entries) and scale 24 (8.9 M vertices,
+  521 M CSR entries, the R-MAT 24 configuration): labels and change counts equal the
+  multi-threaded closed-form oracle after each of the ten iterations.
 """
 import numpy as np
 import pytest
@@ -19,7 +15,9 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 
-def _rmat_host(scale, edge_factor):
+def rmat_host(scale, edge_factor):
+    """R-MAT graph (a,b,c,d = .57,.19,.19,.05, seed 1, symmetrised, deduplicated, isolated
+    vertices removed) built on the device, returned as a host Graph."""
     import bench
     import torch
 
@@ -30,60 +28,36 @@ def _rmat_host(scale, edge_factor):
     return g
 
 
-def test_rmat22_every_iteration_equals_the_oracle():
-    g = _rmat_host(22, 16)
-    with galp_gb300.Propagator(g, early_exit=0) as p:
-        for k in (1, 2, 3, 4):
+def check_every_iteration(g, iterations, **opts):
+    """GPU labels and change counts after each iteration in `iterations` (early exit off)
+    against the multi-threaded closed-form oracle stepped from vertex IDs."""
+    want = np.arange(g.n, dtype=np.int32)
+    counts = []
+    policy, bpow = opts.get("policy", 0), opts.get("buffer_pow", 24)
+    with galp_gb300.Propagator(g, early_exit=0, **opts) as p:
+        for k in range(1, max(iterations) + 1):
+            want, c = oracle.step_par(g.offsets, g.neighbors, want, policy=policy, buffer_pow=bpow)
+            counts.append(c)
+            if k not in iterations:
+                continue
             p.run(k)
-            got, upd = p.get_labels(), list(p.updates)
-            it, want, counts = oracle.run(g.offsets, g.neighbors, k, early_exit=False)
+            got = p.get_labels()
+            assert p.iters_run == k
             assert np.array_equal(got, want), f"iteration {k}: {np.count_nonzero(got != want)} labels differ"
-            assert upd == list(counts)
+            assert list(p.updates) == counts, f"iteration {k}: change counts differ"
 
 
-def _check_step(g, prev, new, sample):
-    off, nbr = g.offsets, g.neighbors
-    deg = off[sample + 1] - off[sample]
-    iso = deg == 0
-    assert np.array_equal(new[sample[iso]], prev[sample[iso]])
-    s = sample[~iso]
-    d = deg[~iso]
-    seg = np.repeat(np.arange(len(s)), d)
-    starts = np.repeat(off[s], d)
-    pos = np.arange(d.sum()) - np.repeat(np.cumsum(d) - d, d)
-    labs = prev[nbr[starts + pos]].astype(np.int64)
-    key = seg.astype(np.int64) << 32 | labs
-    uk, cnt = np.unique(key, return_counts=True)
-    useg = (uk >> 32).astype(np.int64)
-    ulab = (uk & 0xFFFFFFFF).astype(np.int64)
-    wmax = np.zeros(len(s), np.int64)
-    np.maximum.at(wmax, useg, cnt)
-    is_max = cnt == wmax[useg]
-    nmax = np.bincount(useg[is_max], minlength=len(s))
-    # count of the chosen label among the neighbours' labels
-    chosen = new[s].astype(np.int64)
-    ck = np.arange(len(s), dtype=np.int64) << 32 | chosen
-    idx = np.searchsorted(uk, ck)
-    found = (idx < len(uk)) & (uk[np.minimum(idx, len(uk) - 1)] == ck)
-    assert found.all(), f"{np.count_nonzero(~found)} vertices took a label none of their neighbours has"
-    assert np.array_equal(cnt[idx], wmax), "a vertex took a label that is not of maximum count"
-    uniq = nmax == 1
-    best = np.zeros(len(s), np.int64)
-    best[useg[is_max]] = ulab[is_max]  # the only maximum where uniq
-    assert np.array_equal(chosen[uniq], best[uniq])
+def test_rmat22_every_iteration_equals_the_oracle():
+    g = rmat_host(22, 16)
+    check_every_iteration(g, range(1, 11))
 
 
-def test_rmat24_properties_on_a_sample():
-    g = _rmat_host(24, 16)
-    rng = np.random.default_rng(24)
-    sample = np.sort(rng.choice(g.n, 200_000, replace=False))
-    prev = np.arange(g.n, dtype=np.int32)
-    with galp_gb300.Propagator(g, early_exit=0) as p:
-        for k in (1, 2, 3):
-            p.run(k)
-            new = p.get_labels()
-            _check_step(g, prev, new, sample)
-            prev = new
+def test_rmat24_every_iteration_equals_the_oracle():
+    # the R-MAT 24 configuration (edge factor 16): all ten iterations, from the tie-heavy
+    # first ones to the converging last ones
+    g = rmat_host(24, 16)
+    assert g.m > 500_000_000
+    check_every_iteration(g, range(1, 11))
 
 
 def test_lfr_1m_ten_iterations_equal_the_oracle():

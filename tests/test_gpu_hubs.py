@@ -74,3 +74,42 @@ def test_hubs_every_iteration(hub_graph, agg):
 
 def test_hubs_with_frontier(hub_graph):
     _check_every_iteration(hub_graph, 10, frontier=1)
+
+
+def _spread_hubs(g, nh):
+    """The same graph with the hubs (IDs 0..nh-1) moved to evenly spaced IDs, so that under
+    out-of-core batching they sit inside later batches, at nonzero batch-local run positions."""
+    n = g.n
+    pos = np.array([(h + 1) * n // (nh + 1) for h in range(nh)])
+    rest = np.setdiff1d(np.arange(n), pos)
+    perm = np.empty(n, np.int64)  # old ID -> new ID
+    perm[:nh] = pos
+    perm[nh:] = rest
+    src = np.repeat(perm, g.degrees())
+    dst = perm[g.neighbors]
+    order = np.lexsort((dst, src))
+    off = np.zeros(n + 1, np.int64)
+    np.add.at(off, src + 1, 1)
+    return galp_gb300.Graph(np.cumsum(off), dst[order].astype(np.int32)), pos
+
+
+@pytest.mark.parametrize("policy", [1, 2])
+@pytest.mark.parametrize("bpow", [17, 18])
+def test_hubs_inside_out_of_core_batches(hub_graph, policy, bpow):
+    g, pos = _spread_hubs(hub_graph, len(HUBS))
+    deg = g.degrees()
+    assert (deg[pos] > 12288).all()
+    nb, bbs = oracle.batch_boundaries(g.offsets, bpow)
+    assert nb > 1
+    hub_batches = set(np.searchsorted(bbs, pos, side="right") - 1)
+    assert len(hub_batches - {0}) >= 1  # at least one hub in a batch after the first
+    with galp_gb300.Propagator(g, policy=policy, buffer_pow=bpow) as p:
+        for k in range(1, 11):
+            p.run(k)
+            it, want, counts = oracle.run(g.offsets, g.neighbors, k, policy=policy, buffer_pow=bpow)
+            assert p.iters_run == it
+            got = p.get_labels()
+            assert np.array_equal(got, want), f"run({k}): {np.count_nonzero(got != want)} labels differ"
+            assert list(p.updates) == list(counts)
+            if it < k:
+                break

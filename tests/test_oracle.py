@@ -155,3 +155,48 @@ def test_fixed_iteration_count_runs_past_convergence():
     assert np.array_equal(lab_e, lab_f)
     assert list(cnt_f[:it_e]) == list(cnt_e)
     assert (cnt_f[it_e:] <= cnt_e[-1]).all()
+
+
+@pytest.mark.parametrize("TB,ET", [(8, 3), (32, 2), (256, 17)])
+@pytest.mark.parametrize("policy,bpow", [(0, 24), (1, 11), (2, 12)])
+def test_parallel_oracle_equals_sequential(policy, bpow, TB, ET):
+    """The multi-threaded closed form (used at the R-MAT 24/26 sizes) equals the sequential
+    restatement: graphs with ties, hubs, isolated vertices (leading, inner and trailing),
+    small TB/ET so that runs cross chunk, tile, spine-block and level-2 boundaries."""
+    graphs = [galp_gb300.generate_rmat(12, 8, seed=31), galp_gb300.generate_sbm([128] * 12, 10.0, 2.0, seed=5)]
+    g = graphs[1]
+    new_n = g.n + 3
+    iso = np.array([0, 7, new_n - 1])
+    keep = np.setdiff1d(np.arange(new_n), iso)
+    deg = np.zeros(new_n, np.int64)
+    deg[keep] = g.degrees()
+    off = np.zeros(new_n + 1, np.int64)
+    off[1:] = np.cumsum(deg)
+    graphs.append(galp_gb300.Graph(off, keep[g.neighbors].astype(np.int32)))
+    for g in graphs:
+        if policy and oracle.batch_boundaries(g.offsets, bpow)[0] < 0:
+            continue
+        it, lab, cnt = oracle.run(g.offsets, g.neighbors, 8, policy=policy, buffer_pow=bpow, early_exit=False,
+                                  TB=TB, ET=ET)
+        it2, lab2, cnt2 = oracle.run_par(g.offsets, g.neighbors, 8, policy=policy, buffer_pow=bpow,
+                                         early_exit=False, TB=TB, ET=ET)
+        assert it == it2 and np.array_equal(lab, lab2) and np.array_equal(cnt, cnt2)
+        # stepping from given labels is the same update
+        lab3 = np.arange(g.n, dtype=np.int32)
+        for k in range(3):
+            lab3, c = oracle.step_par(g.offsets, g.neighbors, lab3, policy=policy, buffer_pow=bpow, TB=TB, ET=ET)
+            assert c == cnt[k]
+        it4, lab4, _ = oracle.run(g.offsets, g.neighbors, 3, policy=policy, buffer_pow=bpow, early_exit=False,
+                                  TB=TB, ET=ET)
+        assert np.array_equal(lab3, lab4)
+
+
+def test_parallel_oracle_early_exit_and_golden():
+    for path in FIXTURES:
+        z = np.load(path)
+        policy, bpow = int(z["policy"]), int(z["buffer_pow"])
+        it, lab, cnt = oracle.run_par(z["offsets"], z["neighbors"], len(z["counts"]), policy=policy,
+                                      buffer_pow=bpow)
+        assert np.array_equal(lab, z["labels"][it - 1]) and np.array_equal(cnt, z["counts"][:it])
+    g = galp_gb300.generate_sbm([64] * 8, 10.0, 0.5, seed=4)
+    assert oracle.run(g.offsets, g.neighbors, 30)[0] == oracle.run_par(g.offsets, g.neighbors, 30)[0]
