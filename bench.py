@@ -18,6 +18,7 @@ from __future__ import annotations
 import argparse
 import ctypes
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -55,23 +56,85 @@ def _rank_env():
 # workloads
 # ---------------------------------------------------------------------------
 
-def rmat_on_gpu(scale: int, edge_factor: int, seed: int = 1, a=0.57, b=0.19, c=0.19):
-    """R-MAT graph built on the device: raw edges from the library's counter-based
-    sampler (same edges as the CPU generator), then symmetrise, drop self-loops and
-    duplicates, delete isolated vertices and compact IDs.  Returns device tensors
-    (offsets int64[n+1], neighbors int32[m])."""
+_M64 = (1 << 64) - 1
+
+
+def _s64(x: int) -> int:
+    """An unsigned 64-bit constant as the int64 with the same bits."""
+    x &= _M64
+    return x - (1 << 64) if x >> 63 else x
+
+
+def _shr(x, k: int):
+    """Logical right shift of int64 tensors holding unsigned 64-bit values."""
+    return (x >> k) & ((1 << (64 - k)) - 1)
+
+
+def _splitmix64(x):
+    x = x + _s64(0x9E3779B97F4A7C15)
+    x = (x ^ _shr(x, 30)) * _s64(0xBF58476D1CE4E5B9)
+    x = (x ^ _shr(x, 27)) * _s64(0x94D049BB133111EB)
+    return x ^ _shr(x, 31)
+
+
+def _splitmix64_int(x: int) -> int:
+    x = (x + 0x9E3779B97F4A7C15) & _M64
+    x = ((x ^ (x >> 30)) * 0xBF58476D1CE4E5B9) & _M64
+    x = ((x ^ (x >> 27)) * 0x94D049BB133111EB) & _M64
+    return x ^ (x >> 31)
+
+
+def rmat_keys_torch(seed: int, scale: int, e0: int, e1: int, a=0.57, b=0.19, c=0.19, device="cuda"):
+    """Raw R-MAT edge keys (u << 32 | v) of edges [e0, e1) computed with torch only: the
+    counter-based sampler of galp_gb300/csrc/rmat_rng.h restated on int64 tensors (a
+    SplitMix64 finaliser of (seed, edge, level) picks the quadrant at every level; int64
+    multiplication wraps exactly like uint64).  Used where the workload must be built
+    without the library, e.g. for the reference arm."""
     import torch
 
-    import galp_gb300
+    ta, tb, tc = (int(math.floor(x * 4294967296.0 + 0.5)) for x in (a, a + b, a + b + c))
+    base0 = _s64(_splitmix64_int((seed ^ 0x52D4A7F1C3B9E605) & _M64))
+    e = torch.arange(e0, e1, dtype=torch.int64, device=device)
+    base = e * _s64(0x9E3779B97F4A7C15)
+    base ^= base0
+    del e
+    u = torch.zeros_like(base)
+    v = torch.zeros_like(base)
+    for lvl in range(scale):
+        r = _shr(_splitmix64(base + _s64(lvl * 0xD1B54A32D192ED03)), 32)
+        ub = r >= tb
+        vb = ((r >= ta) & (r < tb)) | (r >= tc)
+        u = (u << 1) | ub.to(torch.int64)
+        v = (v << 1) | vb.to(torch.int64)
+    return (u << 32) | v
 
-    L = galp_gb300.load_library()
-    L.galp_gen_rmat_keys_device.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
-                                            ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
-    L.galp_gen_rmat_keys_device.restype = ctypes.c_int
+
+def rmat_on_gpu(scale: int, edge_factor: int, seed: int = 1, a=0.57, b=0.19, c=0.19, sampler: str = "library",
+                device: str = "cuda"):
+    """R-MAT graph built on the device: raw edges from the counter-based sampler (the
+    library's kernel, or its torch restatement with sampler="torch"; both give the CPU
+    generator's edges), then symmetrise, drop self-loops and duplicates, delete isolated
+    vertices and compact IDs.  Returns device tensors (offsets int64[n+1], neighbors
+    int32[m])."""
+    import torch
+
     ne = edge_factor << scale
-    keys = torch.empty(ne, dtype=torch.int64, device="cuda")
-    rc = L.galp_gen_rmat_keys_device(seed, scale, ne, a, b, c, keys.data_ptr(), torch.cuda.current_stream().cuda_stream)
-    assert rc == 0, rc
+    if sampler == "torch":
+        keys = torch.empty(ne, dtype=torch.int64, device=device)
+        step = 1 << 27
+        for e0 in range(0, ne, step):
+            keys[e0:min(ne, e0 + step)] = rmat_keys_torch(seed, scale, e0, min(ne, e0 + step), a, b, c, device)
+    else:
+        import galp_gb300
+
+        L = galp_gb300.load_library()
+        L.galp_gen_rmat_keys_device.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int64, ctypes.c_double,
+                                                ctypes.c_double, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p]
+        L.galp_gen_rmat_keys_device.restype = ctypes.c_int
+        keys = torch.empty(ne, dtype=torch.int64, device="cuda")
+        rc = L.galp_gen_rmat_keys_device(seed, scale, ne, a, b, c, keys.data_ptr(),
+                                         torch.cuda.current_stream().cuda_stream)
+        assert rc == 0, rc
     u = keys >> 32
     v = keys & 0xFFFFFFFF
     del keys
@@ -106,9 +169,10 @@ def rmat_on_gpu(scale: int, edge_factor: int, seed: int = 1, a=0.57, b=0.19, c=0
     for i in range(0, dst.numel(), step):
         nbr[i:i + step] = newid[dst[i:i + step].long()]
     del dst
-    offsets = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    offsets = torch.zeros(n + 1, dtype=torch.int64, device=device)
     offsets[1:] = torch.cumsum(deg[nz], 0)
-    torch.cuda.synchronize()
+    if device != "cpu":
+        torch.cuda.synchronize()
     return offsets, nbr
 
 
@@ -268,15 +332,17 @@ def _propagator_device_nbr(g, nbr_dev, m):
     return p
 
 
-def build_workload(name: str):
-    """Returns (host Graph with pinned arrays when a GPU is present, description)."""
+def build_workload(name: str, library: bool = True):
+    """Returns (host Graph with pinned arrays, description).  library=False builds the
+    graph without loading any of this project's native libraries (the reference arm):
+    R-MAT through the torch restatement of the sampler, edge for edge the same graph."""
     import galp_gb300
 
     kind, prm = WORKLOADS[name]
     if kind == "rmat":
         import torch
 
-        off_d, nbr_d = rmat_on_gpu(prm["scale"], prm["edge_factor"])
+        off_d, nbr_d = rmat_on_gpu(prm["scale"], prm["edge_factor"], sampler="library" if library else "torch")
         off_h = torch.empty(off_d.numel(), dtype=torch.int64, pin_memory=True)
         nbr_h = torch.empty(nbr_d.numel(), dtype=torch.int32, pin_memory=True)
         off_h.copy_(off_d)
@@ -287,6 +353,9 @@ def build_workload(name: str):
         g._pinned = (off_h, nbr_h)  # keep the pinned storage alive
         desc = dict(workload=f"rmat-scale{prm['scale']}-ef{prm['edge_factor']}", a=0.57, b=0.19, c=0.19,
                     seed=1, symmetrised=True, dedup=True, isolated_removed=True)
+    elif not library:
+        raise SystemExit(f"--impl reference: workload {name} is generated by the project's native generator; "
+                         "use an R-MAT workload")
     elif kind == "lfr":
         g = galp_gb300.generate_lfr(prm["n"], seed=1)
         desc = dict(workload="lfr-style-n1M", tau1=2.5, mean_deg=20, max_deg=1000, tau2=1.5, cmin=20, cmax=1000,
@@ -369,24 +438,57 @@ def ncu_traffic(workload: str, group: str):
     return None
 
 
-def cpu_sample(g, target_s: float = 12.0, threads: int = 0):
-    """Time the reference's CPU update on a bounded prefix of the vertices sized for
-    about target_s seconds (one sweep, labels from vertex IDs)."""
+CPU_SAMPLE_ENTRIES = 1 << 28  # CSR entries of the strided CPU sample (about 4 s per 3 sweeps on 16 cores)
+CPU_SAMPLE_SWEEPS = 3
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def cpu_sample_stride(m: int) -> int:
+    """Vertex stride of the CPU sample: every stride-th vertex, about CPU_SAMPLE_ENTRIES
+    CSR entries in expectation; a function of the graph only, so both arms time the same
+    vertices."""
+    return max(1, int(round(m / CPU_SAMPLE_ENTRIES)))
+
+
+def cpu_sample(g, threads: int = 0):
+    """Time the reference's CPU update (port of CPUWorker::update_label, OpenMP dynamic
+    schedule over all host cores, OMP_PROC_BIND=true as the reference's experiment
+    scripts set it) for CPU_SAMPLE_SWEEPS in-place sweeps (iterations 1-3, labels from
+    vertex IDs) over the strided vertex sample."""
+    os.environ.setdefault("OMP_PROC_BIND", "true")  # read when the port's OpenMP runtime loads
     import oracle
 
-    n, m = g.n, g.m
-    off = np.asarray(g.offsets)
-    # calibrate on ~1% of the edges (at least 2M)
-    e_cal = min(m, max(2_000_000, m // 100))
-    v_cal = int(np.searchsorted(off, e_cal))
-    v_cal = max(1, min(n, v_cal))
-    secs, used, _, _ = oracle.cpu_baseline(off, g.neighbors, 1, 0, v_cal, threads)
-    rate = (off[v_cal] - off[0]) / max(secs, 1e-6)
-    e_tgt = min(m, int(rate * target_s))
-    v_s = max(1, min(n, int(np.searchsorted(off, e_tgt))))
-    secs, used, _, _ = oracle.cpu_baseline(off, g.neighbors, 1, 0, v_s, threads)
-    edges = int(off[v_s] - off[0])
-    return dict(seconds=secs, threads=used, edges=edges, vertices=v_s)
+    stride = cpu_sample_stride(g.m)
+    secs, used, edges, _ = oracle.cpu_baseline_strided(g.offsets, g.neighbors, CPU_SAMPLE_SWEEPS, stride, 0, threads)
+    return dict(seconds=secs, threads=used, edges=edges, stride=stride,
+                gteps=CPU_SAMPLE_SWEEPS * edges / max(secs, 1e-9) / 1e9)
+
+
+def cpu_sample_desc(g, s) -> str:
+    return (f"{CPU_SAMPLE_SWEEPS} in-place sweeps (iterations 1-{CPU_SAMPLE_SWEEPS}, labels from vertex IDs) of "
+            f"CPUWorker::update_label (port, std::map counting, OpenMP dynamic schedule, OMP_PROC_BIND=true) "
+            f"over every {s['stride']}-th vertex: {s['edges']} of {g.m} CSR entries per sweep; "
+            f"host CPU: {cpu_model()}, {os.cpu_count()} cores")
 
 
 # ---------------------------------------------------------------------------
@@ -394,24 +496,22 @@ def cpu_sample(g, target_s: float = 12.0, threads: int = 0):
 # ---------------------------------------------------------------------------
 
 def run_reference(args, g, desc, rank, world):
-    res = None
+    """The reference arm: the reference's CPU label update on this host's cores, on the
+    same graph (built without the library) and the same strided sample every step."""
     for _ in range(args.warmup):
-        cpu_sample(g, target_s=args.cpu_seconds / 4)
-    vals = []
+        cpu_sample(g)
+    res = []
     for _ in range(args.steps):
-        s = cpu_sample(g, target_s=args.cpu_seconds)
-        res = s
-        vals.append(s["edges"] / s["seconds"] / 1e9)
-    v = statistics.median(vals)
-    sample = (f"one sweep of CPUWorker::update_label over vertices [0, {res['vertices']}) "
-              f"({res['edges']} CSR entries of {g.m}), labels = vertex IDs")
+        res.append(cpu_sample(g))
+    v = statistics.median(r["gteps"] for r in res)
+    ms = statistics.median(1e3 * r["seconds"] for r in res)
     line = {
         "metric": "GTEPS per LP iteration", "value": round(v, 4), "unit": "GTEPS", "impl": "reference",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic", "config": desc,
-        "ms_per_step": round(1e3 * res["seconds"], 3),
-        "cpu_baseline": {"value": round(v, 4), "unit": "GTEPS", "cores": res["threads"], "kind": "port",
-                         "sample": sample},
+        "ms_per_step": round(ms, 3),
+        "cpu_baseline": {"value": round(v, 4), "unit": "GTEPS", "cores": res[0]["threads"], "kind": "port",
+                         "sample": cpu_sample_desc(g, res[0])},
         "e2e": {"value": round(v, 4), "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
@@ -465,7 +565,9 @@ def run_gpu(args, g, desc, rank, world, dist):
     edges_all = world * NITER * g.m * args.steps
     value = edges_all / (t_max / 1e3) / 1e9
 
-    # roofline of the dominant kernel group
+    # roofline of the dominant kernel group, over dense iterations only: the first
+    # iteration's shortcut (labels = IDs, sorted adjacency lists: one pass that gathers no
+    # labels) is timed as its own group and left out of both groups' averages
     n, m, mb = info.n, info.m, info.m_big
     # algorithmic bytes: 4 B neighbour + 4 B gathered label per CSR entry, 8 B offset,
     # 4 B old + 4 B new label per vertex (8m + 16n + 8 per dense iteration)
@@ -473,20 +575,30 @@ def run_gpu(args, g, desc, rank, world, dist):
     big_bytes = 8 * mb
     shares = {"count_scan_resolve": kt.pipe_ms, "big_vertex_kernels": kt.big_pre_ms + kt.big_post_ms}
     dom = max(shares, key=shares.get)
-    # per iteration: one group per scope (every out-of-core batch is its own scope)
-    iters = max(args.steps * NITER, 1)
     if dom == "count_scan_resolve":
-        dur = kt.pipe_ms / iters
+        dur = kt.pipe_ms / max(kt.pipe_groups, 1)
         alg = pipe_bytes
     else:
-        dur = (kt.big_pre_ms + kt.big_post_ms) / iters
+        dur = (kt.big_pre_ms + kt.big_post_ms) / max(kt.big_pre_groups, 1)
         alg = big_bytes
     achieved = alg / (dur / 1e3) / 1e9
     traffic = ncu_traffic(desc["workload"], dom) if not args.policy else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": int(alg), "avg_launch_ms": round(dur, 4),
+                "launches_averaged": int(kt.pipe_groups if dom == "count_scan_resolve" else kt.big_pre_groups),
                 "kernel_share": {k: round(v / max(sum(shares.values()), 1e-9), 3) for k, v in shares.items()}}
+    it_ms = tools.profile_iterations(p)
+    if not args.policy and len(it_ms) >= NITER:
+        first_short = bool(info.flags & tools.SchedInfo.SORTED)
+        dense = [float(t) for i, t in enumerate(it_ms) if t > 0 and not (first_short and i % NITER == 0)]
+        if dense:
+            it_dense = statistics.mean(dense)
+            whole = (8 * m + 16 * n + 8) / (it_dense / 1e3) / 1e9
+            roofline["whole_iteration"] = {
+                "alg_bytes": int(8 * m + 16 * n + 8), "dense_iteration_ms": round(it_dense, 4),
+                "achieved": round(whole, 1), "frac": round(whole / peak, 4),
+                "first_iteration_ms": round(kt.first_ms / max(kt.first_groups, 1), 4) if kt.first_groups else None}
     if args.policy:  # out-of-core: the neighbours cross the host link every iteration
         roofline["h2d_GBps_per_iteration"] = round(4 * m / (ms_per_step / NITER / 1e3) / 1e9, 1)
     p.close()
@@ -544,13 +656,18 @@ def run_gpu(args, g, desc, rank, world, dist):
         e2e_t = float(t.item())
     e2e_val = world * NITER * g.m / e2e_t / 1e9 if e2e_times else None
 
+    # out-of-core policy 2 on the same graph: 2^24-edge batches streamed from pinned host
+    # memory every iteration, bounded by the host link (reported against its measured peak)
+    policy2 = None
+    if rank == 0 and not args.policy and not args.no_policy2:
+        policy2 = run_policy2(g, dev, stream, args.buffer_pow)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
-        s = cpu_sample(g, target_s=args.cpu_seconds)
-        cpu = {"value": round(s["edges"] / s["seconds"] / 1e9, 4), "unit": "GTEPS", "cores": s["threads"],
-               "kind": "port",
-               "sample": (f"one sweep of CPUWorker::update_label (port) over vertices [0, {s['vertices']}) = "
-                          f"{s['edges']} of {g.m} CSR entries, OpenMP dynamic schedule")}
+        reps = [cpu_sample(g) for _ in range(3)]
+        s = sorted(reps, key=lambda r: r["gteps"])[1]
+        cpu = {"value": round(s["gteps"], 4), "unit": "GTEPS", "cores": s["threads"], "kind": "port",
+               "sample": cpu_sample_desc(g, s) + "; median of 3"}
     cfg = dict(desc)
     cfg.update(iterations_per_step=NITER, early_exit=False, method=0, policy=args.policy,
                l2="inputs larger than L2 (neighbours {:.1f} GB vs 129 MB L2)".format(4 * g.m / 1e9),
@@ -568,10 +685,67 @@ def run_gpu(args, g, desc, rank, world, dist):
         "e2e": {"value": round(e2e_val, 3) if e2e_val else None, "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "seconds_per_step": round(e2e_t, 4) if e2e_times else None},
         "dispatch": dispatch,
+        "policy2": policy2,
         "gpu_launches": int(launches_timed),
         "iteration_ms": round(ms_per_step / NITER, 4),
     }
     return line
+
+
+def pinned_h2d_peak(nbytes: int = 1 << 31, reps: int = 5) -> float:
+    """Host-to-device copy bandwidth (GB/s) of one plain cudaMemcpyAsync of a pinned host
+    buffer (torch copy_), best of reps, timed by CUDA events on its stream."""
+    import torch
+
+    src = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    dst = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.Stream()
+    best = 0.0
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st):
+            e0.record(st)
+            dst.copy_(src, non_blocking=True)
+            e1.record(st)
+        e1.synchronize()
+        best = max(best, nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    del src, dst
+    return best
+
+
+def run_policy2(g, dev, stream, buffer_pow: int, steps: int = 2, warmup: int = 1):
+    """Policy 2 (AsyncLP: batches of < 2^buffer_pow edges, pinned double-buffered copies
+    overlapped with compute) over NITER iterations, early exit off."""
+    import torch
+
+    import galp_gb300
+
+    peak = pinned_h2d_peak()
+    t0 = time.perf_counter()
+    q = galp_gb300.Propagator(g, early_exit=0, device=dev, policy=2, buffer_pow=buffer_pow)
+    setup_s = time.perf_counter() - t0
+    q.set_stream(stream.cuda_stream)
+    for _ in range(warmup):
+        q.enqueue(NITER)
+        q.sync()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        q.enqueue(NITER)
+        q.sync()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    q.close()
+    it_ms = ms / NITER
+    link = 4 * g.m / (it_ms / 1e3) / 1e9  # every iteration streams every neighbour once
+    return {"buffer_pow": buffer_pow, "steps": steps, "warmup": warmup, "ms_per_iteration": round(it_ms, 3),
+            "value": round(g.m / (it_ms / 1e3) / 1e9, 3), "unit": "GTEPS",
+            "setup_s": round(setup_s, 2),
+            "roofline": {"bound": "host-to-device link", "achieved": round(link, 1), "unit": "GB/s",
+                         "peak": round(peak, 1), "peak_kind": "measured pinned cudaMemcpyAsync H2D (2 GiB, best of 5)",
+                         "frac": round(link / peak, 4), "alg_bytes_per_iteration": int(4 * g.m)}}
 
 
 def main():
@@ -581,10 +755,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="galp", choices=["galp", "reference"])
     ap.add_argument("--workload", default=os.environ.get("GALP_BENCH_WORKLOAD", "rmat26"), choices=list(WORKLOADS))
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-dispatch", action="store_true")
+    ap.add_argument("--no-policy2", action="store_true", help="skip the out-of-core policy-2 sub-record")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched (4096 SBM graphs) sub-record")
     ap.add_argument("--policy", type=int, default=0, choices=[0, 1, 2],
                     help="1/2: out-of-core, neighbours streamed from pinned host memory in 2^buffer_pow chunks")
     ap.add_argument("--buffer-pow", type=int, default=24)
@@ -603,7 +778,7 @@ def main():
 
         if torch.cuda.is_available():
             torch.cuda.set_device(local)
-        g, desc = build_workload(args.workload)
+        g, desc = build_workload(args.workload, library=False)
         print(json.dumps(run_reference(args, g, desc, rank, world)))
         return 0
 
@@ -638,6 +813,16 @@ def main():
         return 0
     g, desc = build_workload(args.workload)
     line = run_gpu(args, g, desc, rank, world, dist)
+    if rank == 0 and not args.no_batch and not args.policy and WORKLOADS[args.workload][0] == "rmat":
+        # batched mode (4096 SBM graphs in one CUDA-graph launch vs per-graph launches)
+        import gc
+
+        del g
+        gc.collect()
+        torch.cuda.empty_cache()
+        b = run_batch(argparse.Namespace(steps=3, warmup=3), WORKLOADS["batch4096"][1]["count"])
+        line["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "steps", "warmup", "config",
+                                              "batched_vs_sequential", "clocks")}
     if rank == 0:
         print(json.dumps(line))
     if dist:

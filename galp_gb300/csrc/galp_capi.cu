@@ -882,7 +882,7 @@ int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
             int e0 = prof.on ? prof.mark(st) : -1;
             first_iteration_kernel<<<(int)std::min<int64_t>((n + kTB - 1) / kTB, (int64_t)sms * 8), kTB, 0, st>>>(q, n, m);
             launched("first_iteration_kernel", st);
-            if (prof.on) prof.spans[0].push_back({e0, prof.mark(st)});
+            if (prof.on) prof.spans[3].push_back({e0, prof.mark(st)});
             full_state = false;  // the shortcut leaves no per-vertex counts behind
         } else {
             if ((rc = enqueue_scope(st, sched.scopes[0], (const int32_t *)b_nbr[0].p, lab[it & 1], lab[(it + 1) & 1],
@@ -1438,6 +1438,7 @@ int galp_batch_tune(galp_ctx *ctx, int32_t niter, galp_tune_result *res)
     E.prof.spans[0].clear();
     E.prof.spans[1].clear();
     E.prof.spans[2].clear();
+    E.prof.spans[3].clear();
     E.prof.it_spans.clear();
     E.prof.used = 0;
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);  // recapture with the chosen shapes
@@ -1475,7 +1476,9 @@ int galp_profile_read(galp_ctx *ctx, galp_kernel_times *out)
     out->big_pre_groups = P.group_n[1];
     out->big_post_ms = P.group_ms[2];
     out->big_post_groups = P.group_n[2];
-    for (int g = 0; g < 3; ++g) {
+    out->first_ms = P.group_ms[3];
+    out->first_groups = P.group_n[3];
+    for (int g = 0; g < 4; ++g) {
         P.group_ms[g] = 0;
         P.group_n[g] = 0;
     }

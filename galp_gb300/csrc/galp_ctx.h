@@ -94,11 +94,12 @@ struct Profiler {
     int level = 0;
     std::vector<cudaEvent_t> pool;
     size_t used = 0;
-    std::vector<std::pair<int, int>> spans[3];  // 0 = count/scan/resolve, 1 = big pre, 2 = big post
+    // 0 = count/scan/resolve, 1 = big pre, 2 = big post, 3 = first-iteration shortcut
+    std::vector<std::pair<int, int>> spans[4];
     int last = -1;                              // level 2: mark that the next interval starts at
     std::vector<std::pair<const char *, std::pair<int, int>>> kspans;
-    double group_ms[3] = {0, 0, 0};
-    int group_n[3] = {0, 0, 0};
+    double group_ms[4] = {0, 0, 0, 0};
+    int group_n[4] = {0, 0, 0, 0};
     std::vector<std::pair<const char *, std::pair<double, int64_t>>> kstats;  // name -> (ms, launches)
     std::vector<std::pair<int, int>> it_spans;  // in-core iterations
     std::vector<float> it_ms;
@@ -127,7 +128,7 @@ struct Profiler {
     // wait for the recorded events and fold their intervals into the totals
     void fold()
     {
-        for (int g = 0; g < 3; ++g) {
+        for (int g = 0; g < 4; ++g) {
             for (auto &sp : spans[g]) {
                 float t = 0.f;
                 if (sp.first >= 0 && sp.second >= 0 &&

@@ -20,7 +20,8 @@ class SchedInfo(ctypes.Structure):
 class KernelTimes(ctypes.Structure):
     _fields_ = [("pipe_ms", ctypes.c_double), ("pipe_groups", ctypes.c_int32), ("big_pre_groups", ctypes.c_int32),
                 ("big_pre_ms", ctypes.c_double), ("big_post_ms", ctypes.c_double),
-                ("big_post_groups", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("big_post_groups", ctypes.c_int32), ("first_groups", ctypes.c_int32),
+                ("first_ms", ctypes.c_double)]
 
 
 class Variant(ctypes.Structure):

@@ -41,7 +41,9 @@ typedef struct {
     double big_pre_ms;     /* big_insert + big_stats + big_dcnt: summed device time */
     double big_post_ms;    /* big_resolve + big_clear + big_reset */
     int32_t big_post_groups;
-    int32_t pad;
+    int32_t first_groups;  /* first-iteration shortcuts timed */
+    double first_ms;       /* first_iteration_kernel (labels = IDs, sorted adjacency): summed
+                              device time; not part of pipe_ms */
 } galp_kernel_times;
 
 typedef struct {

@@ -195,6 +195,10 @@ def _load_port():
         L.cpu_lp_run.restype = ctypes.c_int64
         L.cpu_lp_run.argtypes = [ctypes.c_int64, P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                  P, P, ctypes.POINTER(ctypes.c_double)]
+        L.cpu_lp_run_strided.restype = ctypes.c_int64
+        L.cpu_lp_run_strided.argtypes = [ctypes.c_int64, P, P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                         ctypes.c_int, P, P, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_int64)]
         L.cpu_lp_threads.restype = ctypes.c_int
         L.cpu_lp_threads.argtypes = []
         _port = L
@@ -216,3 +220,20 @@ def cpu_baseline(offsets, neighbors, niter: int, v_begin: int = 0, v_end: int | 
     used = L.cpu_lp_run(n, off.ctypes.data, nbr.ctypes.data, v_begin, v_end, niter, threads, lab.ctypes.data,
                         cnt.ctypes.data, ctypes.byref(secs))
     return secs.value, int(used), lab[:n], cnt[:niter]
+
+
+def cpu_baseline_strided(offsets, neighbors, niter: int, stride: int, phase: int = 0, threads: int = 0):
+    """Time niter in-place sweeps of the reference's CPU update over the strided vertex
+    sample phase, phase + stride, ...  Returns (seconds, threads_used, sample CSR entries,
+    counts)."""
+    L = _load_port()
+    off = np.ascontiguousarray(offsets, dtype=np.int64)
+    nbr = np.ascontiguousarray(neighbors, dtype=np.int32)
+    n = len(off) - 1
+    lab = np.zeros(max(n, 1), np.int32)
+    cnt = np.zeros(max(niter, 1), np.int64)
+    secs = ctypes.c_double()
+    edges = ctypes.c_int64()
+    used = L.cpu_lp_run_strided(n, off.ctypes.data, nbr.ctypes.data, stride, phase, niter, threads, lab.ctypes.data,
+                                cnt.ctypes.data, ctypes.byref(secs), ctypes.byref(edges))
+    return secs.value, int(used), int(edges.value), cnt[:niter]
