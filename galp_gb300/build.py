@@ -5,6 +5,7 @@ Products (all under galp_gb300/lib/ unless noted):
   libgalp_gen.so   seeded graph generators behind include/galp_gen.h
   libgalp_host.so  front end: .txt/.bin loaders and accuracy measures (include/galp_host.h)
   galp             the command-line front end (src mirrors the reference's main.cu CLI)
+  galp_convert     edge-list converters (the reference's utils/edgelist2bin.cpp, normalize.py)
 and the test-infrastructure oracle:
   oracle/_build/liblp_oracle.so   CPU restatement of the reference update
   oracle/_ref/ref_harness         reference kernels run on the CPU (only where the
@@ -31,6 +32,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CUDA_SOURCES = ["galp_capi.cu", "galp_tools.cu", "galp_noalloc.cu", "galp_mlp.cu"]
 HOST_SOURCES = ["host/graph_io.cpp", "host/accuracy.cpp"]
+
+
+def reference_tree() -> str:
+    """The reference source tree the oracle's reference harness is built from:
+    $GALP_REFERENCE, else a directory named "reference" beside the repository."""
+    return os.environ.get("GALP_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 
 
 def _run(cmd: list[str]) -> tuple[list[str], int, str]:
@@ -78,6 +85,10 @@ def build(force: bool = False, verbose: bool = False) -> None:
     jobs.append((gen_out, [gen_src, os.path.join(inc, "galp_gen.h")],
                  ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-o", gen_out, gen_src]))
 
+    conv_src = os.path.join(PKG, "host", "convert.cpp")
+    conv_out = os.path.join(LIB, "galp_convert")
+    jobs.append((conv_out, [conv_src], ["g++", "-O2", "-std=c++17", "-o", conv_out, conv_src]))
+
     host_srcs = [os.path.join(PKG, s) for s in HOST_SOURCES]
     host_out = os.path.join(LIB, "libgalp_host.so")
     if all(os.path.exists(s) for s in host_srcs):
@@ -116,8 +127,9 @@ def build(force: bool = False, verbose: bool = False) -> None:
 def _run_jobs(jobs, force: bool, verbose: bool, extra_ref: bool) -> list[str]:
     todo = [(o, cmd) for o, deps, cmd in jobs if force or not _newer(o, deps)]
     ref_script = os.path.join(ORACLE, "build_ref.sh")
-    ref_needed = extra_ref and os.path.isdir(os.environ.get("GALP_REFERENCE", "/root/reference")) and (
-        force or not _newer(os.path.join(ORACLE, "_ref", "ref_harness"), _deps(os.path.join(ORACLE, "refsim"))))
+    ref_deps = _deps(os.path.join(ORACLE, "refsim")) + [ref_script]
+    ref_needed = extra_ref and os.path.isdir(reference_tree()) and (
+        force or not all(_newer(os.path.join(ORACLE, "_ref", t), ref_deps) for t in ("ref_harness", "edgelist2bin")))
     with ThreadPoolExecutor(max_workers=max(1, len(todo) + 1)) as ex:
         futs = [ex.submit(_run, cmd) for _, cmd in todo]
         if ref_needed:

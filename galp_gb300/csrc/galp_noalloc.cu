@@ -3,8 +3,11 @@
 // Some callers cannot call cudaMalloc: code that runs under an external allocator
 // that owns all device memory, plugins loaded into a host framework that forbids
 // allocation outside its pool, and latency-critical paths where an allocation (and
-// its implicit synchronisation) is not acceptable.  galp_run_noalloc serves them: it
-// runs the same exact update kernel as galp_run, but every device buffer it needs --
+// its implicit synchronisation) is not acceptable.  galp_run_noalloc serves them.  It
+// runs a different kernel from galp_run -- the single-pass tile kernel (lp_tile_kernel:
+// counting, run bases by decoupled look-back and resolution in one launch per
+// iteration) instead of the degree-bucketed count/scan/resolve pipeline -- with the
+// same labels, iteration counts and change counts.  Every device buffer it needs --
 // the copy of the graph, both label buffers, the tile schedule, the look-back status
 // words and the control block -- lives in one file-scope static device array of
 // kScratchBytes (12.5 MiB), which every GPU that loads the library holds until the
@@ -15,12 +18,21 @@
 // above 2048 neighbours (those need the global-table path, whose tables are sized per
 // graph).  Larger graphs are rejected with GALP_EUNSUPPORTED.
 //
-// Set-up: the first call on a device (with that device current) takes the device
-// address of the static array with cudaGetSymbolAddress and caches it; host code
-// must not use the array's name as a pointer.  That first call should come before any
-// stream capture.  All calls on a device share the one array and the array keeps the
-// last call's contents; each call clears or overwrites what it reads.  Calls that
-// overlap on the GPU race on it; calls from one process are serialised per device.
+// Set-up: every call looks up the device address of the static array with
+// cudaGetSymbolAddress (the array's name is a host-side stand-in in host code); the
+// first call on a device, or the first after the device's context was reset, also
+// clears the status words.  A call
+// must never be made on a stream that is being captured: it copies from pageable host
+// memory and synchronises the stream, so it checks and returns GALP_EUNSUPPORTED.
+// All calls on a device share the one array and the array keeps the last call's
+// contents; each call clears or overwrites what it reads.  Calls that overlap on the
+// GPU race on it; calls from one process are serialised per device, and every call
+// (on success and on error) waits for the work it queued before it returns.
+//
+// Failure detection: every look-back wait is bounded (kSpinLimit polls by default);
+// a wait that runs out sets an error bit and the kernel returns, and the call reports
+// GALP_ETIMEOUT.  galp_debug_noalloc_lookback (tests only) lowers the bound and makes
+// the waits expect a status epoch that no tile publishes, so that they run out.
 #include <cuda_runtime.h>
 
 #include <climits>
@@ -69,6 +81,12 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 namespace {
 
 constexpr int kMaxDevices = 64;
+
+// failure-detection test hook (galp_debug_noalloc_lookback)
+std::mutex g_debug_mu;
+long long g_spin_limit = galp::kSpinLimit;
+bool g_wait_unset = false;
+
 struct DeviceState {
     std::mutex mu;
     unsigned char *base = nullptr;  // device address of g_noalloc_scratch on this device
@@ -77,16 +95,21 @@ struct DeviceState {
 };
 DeviceState g_dev[kMaxDevices];
 
-// Once per device, with the device current: the array's device address, the tile
-// kernel's shared-memory opt-in and its grid, and a cleared status area.
+// Every call, with the device current: the array's device address and the tile
+// kernel's shared-memory opt-in.  When the address differs from the one recorded (first
+// call on the device, or a new context after a device reset reloaded the module), also
+// the tile kernel's grid and a cleared status area.
 int setup_device(int dev, DeviceState &D, cudaStream_t st)
 {
-    if (D.base) return GALP_OK;
     void *ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return GALP_ECUDA;
+    // a context-level attribute: set on every call, so a reset context gets it again
     if (cudaFuncSetAttribute(galp::lp_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)sizeof(TileSmem)) != cudaSuccess)
         return GALP_ECUDA;
+    if (D.base == (unsigned char *)ptr) return GALP_OK;
+    D.base = nullptr;
+    D.epoch = 0;
     int sms = 0, occ = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return GALP_ECUDA;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, galp::lp_tile_kernel, galp::kTB, sizeof(TileSmem)) !=
@@ -126,6 +149,14 @@ struct Stager {
 
 }  // namespace
 
+extern "C" int galp_debug_noalloc_lookback(int64_t spin_limit, int32_t wait_unset)
+{
+    std::lock_guard<std::mutex> lock(g_debug_mu);
+    g_spin_limit = spin_limit > 0 ? (long long)spin_limit : galp::kSpinLimit;
+    g_wait_unset = wait_unset != 0;
+    return GALP_OK;
+}
+
 extern "C" int galp_run_noalloc(const galp_csr *g, int32_t niter, int32_t early_exit, int32_t *labels_out,
                                 galp_stats *stats, void *stream)
 {
@@ -143,10 +174,31 @@ extern "C" int galp_run_noalloc(const galp_csr *g, int32_t niter, int32_t early_
     if (cudaGetDevice(&dev) != cudaSuccess) return GALP_ENODEV;
     if (dev < 0 || dev >= kMaxDevices) return GALP_EUNSUPPORTED;
     cudaStream_t st = (cudaStream_t)stream;
+    // never on a capturing stream (pageable copies and stream synchronisation)
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        (void)cudaGetLastError();
+        return GALP_EUNSUPPORTED;
+    }
+    long long spin_limit;
+    bool wait_unset;
+    {
+        std::lock_guard<std::mutex> lock(g_debug_mu);
+        spin_limit = g_spin_limit;
+        wait_unset = g_wait_unset;
+    }
     DeviceState &D = g_dev[dev];
     std::lock_guard<std::mutex> lock(D.mu);
+    (void)cudaGetLastError();  // an earlier, unrelated runtime error must not be reported as ours
+    // after work has been queued, every error return first waits for it (best effort), so
+    // that no kernel of this call still uses the shared array when the next call starts
+    auto fail = [&](int code) {
+        (void)cudaStreamSynchronize(st);
+        (void)cudaGetLastError();
+        return code;
+    };
     int rc = setup_device(dev, D, st);
-    if (rc) return rc;
+    if (rc) return fail(rc);
 
     const int64_t n = g->n, m = g->m;
     unsigned char *B = D.base;
@@ -163,9 +215,9 @@ extern "C" int galp_run_noalloc(const galp_csr *g, int32_t niter, int32_t early_
 
     // graph
     if (m && cudaMemcpyAsync(d_nbr, g->neighbors, sizeof(int32_t) * m, cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return GALP_ECUDA;
+        return fail(GALP_ECUDA);
     if (cudaMemcpyAsync(d_off, g->offsets, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st) != cudaSuccess)
-        return GALP_ECUDA;
+        return fail(GALP_ECUDA);
 
     // tile schedule (same packing rule as the allocating path), streamed to the device
     int64_t ntiles = 0;
@@ -218,20 +270,22 @@ extern "C" int galp_run_noalloc(const galp_csr *g, int32_t niter, int32_t early_
         tv0.flush();
         tbig.flush();
         tused.flush();
-        if (vpos.err || tv0.err || tbig.err || tused.err) return GALP_ECUDA;
+        if (vpos.err || tv0.err || tbig.err || tused.err) return fail(GALP_ECUDA);
     }
 
     // neighbours in range before any iteration reads labels through them
-    if (cudaMemsetAsync(d_bad, 0, sizeof(int), st) != cudaSuccess) return GALP_ECUDA;
+    if (cudaMemsetAsync(d_bad, 0, sizeof(int), st) != cudaSuccess) return fail(GALP_ECUDA);
     if (m) galp::validate_kernel<<<256, 256, 0, st>>>(d_nbr, m, n, d_bad);
+    if (cudaGetLastError() != cudaSuccess) return fail(GALP_ECUDA);
     int bad = 0;
-    if (cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return GALP_ECUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return GALP_ECUDA;
-    if (bad) return GALP_EFORMAT;
+    if (cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return fail(GALP_ECUDA);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(GALP_ECUDA);
+    if (bad) return fail(GALP_EFORMAT);
 
     const long long thr = early_exit ? (long long)std::floor((double)n * 1e-5) : -1;
     if (n) galp::init_labels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(lab[0], n);
     galp::init_ctl_kernel<<<1, 1, 0, st>>>(d_ctl, thr, niter);
+    if (cudaGetLastError() != cudaSuccess) return fail(GALP_ECUDA);
     IterArgs a{};
     a.nbr = d_nbr;
     a.off = d_off;
@@ -243,26 +297,31 @@ extern "C" int galp_run_noalloc(const galp_csr *g, int32_t niter, int32_t early_
     a.last_v = last_v;
     a.status = d_status;
     a.ctl = d_ctl;
+    a.spin_limit = spin_limit;
+    a.wait_xor = wait_unset ? 1u : 0u;
     const int grid = (int)(ntiles < D.grid ? ntiles : D.grid);
     for (int it = 0; it < niter; ++it) {
         a.lab_in = lab[it & 1];
         a.lab_out = lab[(it + 1) & 1];
-        if (++D.epoch > (unsigned)galp::kEpochMask) {
-            D.epoch = 1;
-            if (cudaMemsetAsync(d_status, 0, sizeof(unsigned long long) * kMaxV, st) != cudaSuccess) return GALP_ECUDA;
+        // the test hook clears the status words every iteration, so that only this
+        // iteration's epoch is present and epoch ^ 1 is published by no tile
+        if (++D.epoch > (unsigned)galp::kEpochMask || wait_unset) {
+            if (D.epoch > (unsigned)galp::kEpochMask) D.epoch = 1;
+            if (cudaMemsetAsync(d_status, 0, sizeof(unsigned long long) * kMaxV, st) != cudaSuccess)
+                return fail(GALP_ECUDA);
         }
         a.epoch = D.epoch;
-        if (cudaMemsetAsync(&d_ctl->ticket, 0, sizeof(unsigned long long), st) != cudaSuccess) return GALP_ECUDA;
+        if (cudaMemsetAsync(&d_ctl->ticket, 0, sizeof(unsigned long long), st) != cudaSuccess) return fail(GALP_ECUDA);
         if (grid > 0) galp::lp_tile_kernel<<<grid, galp::kTB, sizeof(TileSmem), st>>>(a);
         galp::finalize_kernel<<<1, 1, 0, st>>>(d_ctl);
+        if (cudaGetLastError() != cudaSuccess) return fail(GALP_ECUDA);
     }
-    if (cudaGetLastError() != cudaSuccess) return GALP_ECUDA;
     Ctl c;
-    if (cudaMemcpyAsync(&c, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st) != cudaSuccess) return GALP_ECUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return GALP_ECUDA;
+    if (cudaMemcpyAsync(&c, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st) != cudaSuccess) return fail(GALP_ECUDA);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(GALP_ECUDA);
     if (n && cudaMemcpyAsync(labels_out, lab[c.iter & 1], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess)
-        return GALP_ECUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess) return GALP_ECUDA;
+        return fail(GALP_ECUDA);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return fail(GALP_ECUDA);
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->iters_run = c.iter;

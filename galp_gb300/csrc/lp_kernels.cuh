@@ -37,7 +37,7 @@ constexpr int kBigChunk = 1024;       // edges per big_insert CTA
 constexpr int kBigSlotChunk = 8192;   // occupied-list entries per big_stats CTA
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
-constexpr long long kSpinLimit = 1ll << 20;  // look-back give-up bound (about a second)
+constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound (about a second)
 
 // error bits in Ctl::err
 constexpr int kErrLookback = 1;
@@ -92,6 +92,8 @@ struct IterArgs {
     int32_t *lab_out;
     unsigned long long *status;
     unsigned epoch;
+    unsigned wait_xor;          // look-back accepts statuses of epoch ^ wait_xor (0; tests only)
+    long long spin_limit;       // look-back polls before a wait gives up
     Ctl *ctl;
     // big vertices
     int32_t nbig;
@@ -160,56 +162,6 @@ __device__ __forceinline__ long long warp_sum_ll(long long v)
     return v;
 }
 
-// ---------------------------------------------------------------------------
-// decoupled look-back (executed by one full warp)
-// ---------------------------------------------------------------------------
-__device__ long long lookback_prefix(unsigned long long *status, long long t, unsigned epoch,
-                                     long long D, int lane, Ctl *ctl)
-{
-    if (t == 0) {
-        if (lane == 0) st_relaxed_u64(&status[0], pack_status(2, epoch, (unsigned long long)D));
-        return 0;
-    }
-    if (lane == 0) st_relaxed_u64(&status[t], pack_status(1, epoch, (unsigned long long)D));
-    const unsigned ep = epoch & kEpochMask;
-    long long P = 0;
-    long long j = t - 1;
-    for (;;) {
-        const long long jj = j - lane;
-        unsigned long long w;
-        unsigned state;
-        if (jj >= 0) {
-            long long spins = 0;
-            unsigned ns = 32;
-            for (;;) {
-                w = ld_relaxed_u64(&status[jj]);
-                state = (unsigned)(w >> kStateShift);
-                if (state != 0 && (unsigned)((w >> kEpochShift) & kEpochMask) == ep) break;
-                // give up after kSpinLimit polls, or at once when another wait already gave up
-                if (++spins > kSpinLimit || *((volatile int *)&ctl->err)) {
-                    atomicOr(&ctl->err, kErrLookback);
-                    state = 2;
-                    w = 0;
-                    break;
-                }
-                __nanosleep(ns);
-                if (ns < 1024) ns <<= 1;
-            }
-        } else {
-            state = 2;
-            w = 0;
-        }
-        const unsigned pm = __ballot_sync(kFull, state == 2);
-        const int lim = pm ? (__ffs(pm) - 1) : 31;
-        long long val = (lane <= lim) ? (long long)(w & kValueMask) : 0;
-        P += warp_sum_ll(val);
-        if (pm) break;
-        j -= 32;
-    }
-    if (lane == 0) st_relaxed_u64(&status[t], pack_status(2, epoch, (unsigned long long)(P + D)));
-    return P;
-}
-
 // Block-wide decoupled look-back: all kTB threads read kTB predecessors per round
 // trip, so a tile whose nearest published prefix lies a few hundred tiles back (the
 // usual case with hundreds of resident CTAs) waits for one or two L2 round trips.
@@ -221,8 +173,12 @@ struct LookbackSmem {
     int done;
 };
 
+// A wait gives up after spin_limit polls (or at once when another wait already gave
+// up), sets kErrLookback and takes a zero prefix, so the kernel always returns; the host
+// reports the error.  The wait accepts statuses of epoch (epoch ^ wait_xor): wait_xor is
+// 0 except in the failure-detection test, where no tile publishes that epoch.
 __device__ long long lookback_prefix_block(unsigned long long *status, long long t, unsigned epoch, long long D,
-                                           Ctl *ctl, LookbackSmem &L)
+                                           Ctl *ctl, LookbackSmem &L, long long spin_limit, unsigned wait_xor)
 {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (t == 0) {
@@ -230,7 +186,7 @@ __device__ long long lookback_prefix_block(unsigned long long *status, long long
         return 0;
     }
     if (tid == 0) st_relaxed_u64(&status[t], pack_status(1, epoch, (unsigned long long)D));
-    const unsigned ep = epoch & kEpochMask;
+    const unsigned ep = (epoch ^ wait_xor) & kEpochMask;
     long long P = 0;
     long long j = t - 1;
     for (;;) {
@@ -244,8 +200,8 @@ __device__ long long lookback_prefix_block(unsigned long long *status, long long
                 w = ld_relaxed_u64(&status[jj]);
                 state = (unsigned)(w >> kStateShift);
                 if (state != 0 && (unsigned)((w >> kEpochShift) & kEpochMask) == ep) break;
-                // give up after kSpinLimit polls, or at once when another wait already gave up
-                if (++spins > kSpinLimit || *((volatile int *)&ctl->err)) {
+                // give up after spin_limit polls, or at once when another wait already gave up
+                if (++spins > spin_limit || *((volatile int *)&ctl->err)) {
                     atomicOr(&ctl->err, kErrLookback);
                     state = 2;
                     w = 0;
@@ -579,7 +535,7 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
         if (bi >= 0) {
             // single big vertex: its distinct count was computed by big_insert
             const long long D = *((volatile int *)&p.bstat[bi].d);
-            const long long P = lookback_prefix_block(p.status, t, p.epoch, D, p.ctl, S.lb);
+            const long long P = lookback_prefix_block(p.status, t, p.epoch, D, p.ctl, S.lb, p.spin_limit, p.wait_xor);
             if (tid == 0) {
                 p.big_a[bi] = P;
                 if (v0 == p.last_v) p.ctl->N = P + D;
@@ -852,7 +808,7 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
         // P6: the tile's run base by block-wide look-back, then the vertices whose
         // winner is unique (no position needed)
         {
-            const long long P = lookback_prefix_block(p.status, t, p.epoch, S.D, p.ctl, S.lb);
+            const long long P = lookback_prefix_block(p.status, t, p.epoch, S.D, p.ctl, S.lb, p.spin_limit, p.wait_xor);
             if (tid == 0) {
                 S.P = P;
                 if (p.last_v >= v0 && p.last_v < v1) {

@@ -112,17 +112,23 @@ int galp_sync(galp_ctx *ctx, galp_stats *stats);
 /* Label propagation without device allocation, for callers that cannot call
  * cudaMalloc (a host framework or external allocator owns all device memory, or an
  * allocation's synchronisation is not acceptable on the calling path).  No
- * counterpart in the reference.  Same update and labels as galp_create + galp_run +
- * galp_get_labels with method 0, policy 0, but every device buffer lives in one
- * static device array of 12.5 MiB that each GPU loading the library holds until the
- * process exits; nothing is allocated on the device or the host.
+ * counterpart in the reference.  Same labels, iteration count and change counts as
+ * galp_create + galp_run + galp_get_labels with method 0, policy 0 (computed by a
+ * different kernel: one single-pass tile kernel per iteration), but every device
+ * buffer lives in one static device array of 12.5 MiB that each GPU loading the
+ * library holds until the process exits; nothing is allocated on the device or the
+ * host.
  *   graph       host CSR; at most GALP_NOALLOC_MAX_VERTICES vertices, at most
  *               GALP_NOALLOC_MAX_ENTRIES entries, no vertex above 2048 neighbours
  *               (GALP_EUNSUPPORTED otherwise)
  *   labels_out  host int32[n]; stats may be NULL; stream: cudaStream_t or NULL
- * The first call on a device (with that device current) sets up the array's address
- * and should come before any stream capture.  Calls on a device share the array;
- * calls that overlap on the GPU race on it (calls from one process are serialised). */
+ * Every call looks up the array's device address (cudaGetSymbolAddress, with the
+ * call's device current) and waits for the work it queued before it returns, on
+ * success and on error.  Never call it on a stream that is being captured (it copies
+ * from pageable memory and synchronises; it returns GALP_EUNSUPPORTED there).  Calls
+ * on a device share the array; calls that overlap on the GPU race on it (calls from
+ * one process are serialised).  GALP_ETIMEOUT: a look-back wait of the kernel ran out
+ * (bounded waits; the kernel returned and the labels are not valid). */
 #define GALP_NOALLOC_MAX_VERTICES (1 << 17)
 #define GALP_NOALLOC_MAX_ENTRIES (1 << 21)
 int galp_run_noalloc(const galp_csr *graph, int32_t niter, int32_t early_exit, int32_t *labels_out,

@@ -126,6 +126,12 @@ int galp_profile_read(galp_ctx *ctx, galp_kernel_times *out);
  * cap entries and the number of distinct kernels to *count. */
 int galp_profile_kernels(galp_ctx *ctx, galp_kernel_stat *out, int32_t cap, int32_t *count);
 
+/* Test hook of galp_run_noalloc's failure detection, process-wide: every look-back wait
+ * of later calls gives up after spin_limit polls (<= 0: the default bound), and with
+ * wait_unset != 0 the waits expect a status that no tile publishes, so that they run
+ * out and the call returns GALP_ETIMEOUT.  (0, 0) restores the defaults. */
+int galp_debug_noalloc_lookback(int64_t spin_limit, int32_t wait_unset);
+
 /* Write nedges raw R-MAT edge keys (u << 32 | v) into device memory d_out, on
  * `stream` (cudaStream_t as void*), with the same sampler as galp_gen_rmat. */
 int galp_gen_rmat_keys_device(uint64_t seed, int32_t scale, int64_t nedges, double a, double b, double c,

@@ -32,7 +32,9 @@ def write_bin(g, path):
     np.stack([src, g.neighbors.astype(np.int32)], 1).astype(np.int32).tofile(path)
 
 
-REFERENCE = os.environ.get("GALP_REFERENCE", "/root/reference")
+# the reference tree: $GALP_REFERENCE, else a directory named "reference" beside the repository
+_REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+REFERENCE = os.environ.get("GALP_REFERENCE", os.path.join(os.path.dirname(_REPO), "reference"))
 
 
 def sample_graph():
