@@ -112,30 +112,41 @@ void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
 
 }  // namespace
 
-// Hub table capacity: `per_edge` slots per edge, a multiple of four slots (tables stay on
-// 32-byte sectors).  Four per edge (load <= 1/4) is the default: the probes, one memory
-// round trip per 4-slot group, cost more than the larger footprint.
-constexpr int kHubSlotsPerEdge = 4;
-uint32_t hub_table_slots(int64_t deg, int per_edge)
-{
-    return (uint32_t)std::min<int64_t>((per_edge * deg + 3) & ~(int64_t)3, 0xFFFFFFFCll);
-}
+constexpr int kMaxHubShift = 6;  // at most 64x the default hub partitions
 
-// Re-size every hub table at `per_edge` slots per edge (table offsets, per-scope sizes).
-void resize_hub_tables(Schedule &S, const int64_t *off, int per_edge)
+// Hash partitions of the big vertices: a hub of degree D gets ceil(D * 2^shift / 2048)
+// partitions (its chunks emit at most D pairs, about 2048 per partition while labels are
+// still mostly distinct), each holding 1.5x its share plus 256 pairs, at most
+// kHubPartCap.  Partition indices are global; pair areas are relative to the scope (out-of-
+// core batches reuse one area).
+void plan_hub_parts(Schedule &S, int shift)
 {
-    S.max_table_slots = 0;
+    const size_t nb = S.big_v.size();
+    S.hub_shift = shift;
+    S.hub_p0.assign(nb + 1, 0);
+    S.hub_pbase.assign(nb, 0);
+    S.hub_pcap.assign(nb, 0);
+    S.part_big.clear();
+    S.max_pair_slots = 0;
     for (Scope &sc : S.scopes) {
-        int64_t toff = 0;
+        sc.q0 = (int32_t)S.part_big.size();
+        int64_t pbase = 0;
         for (int32_t b = sc.b0; b < sc.b0 + sc.nb; ++b) {
-            const int32_t v = S.big_v[(size_t)b];
-            S.big_toff[(size_t)b] = toff;
-            S.big_tcap[(size_t)b] = hub_table_slots(off[v + 1] - off[v], per_edge);
-            toff += S.big_tcap[(size_t)b];
+            const int64_t deg = S.big_deg[(size_t)b];
+            const double scaled = std::ldexp((double)deg, shift) / kHubPartPairs;
+            const int64_t np = std::max<int64_t>(1, std::min<int64_t>((int64_t)std::ceil(scaled), deg));
+            const int64_t cap = std::min<int64_t>(kHubPartCap, (3 * deg + 2 * np - 1) / (2 * np) + 256);
+            S.hub_p0[(size_t)b] = (int32_t)S.part_big.size();
+            S.hub_pbase[(size_t)b] = pbase;
+            S.hub_pcap[(size_t)b] = (int32_t)cap;
+            S.part_big.insert(S.part_big.end(), (size_t)np, b);
+            pbase += np * cap;
         }
-        sc.table_slots = toff;
-        S.max_table_slots = std::max(S.max_table_slots, toff);
+        sc.nq = (int32_t)S.part_big.size() - sc.q0;
+        sc.pair_slots = pbase;
+        S.max_pair_slots = std::max(S.max_pair_slots, pbase);
     }
+    S.hub_p0[nb] = (int32_t)S.part_big.size();
 }
 
 // Static per-graph schedule (host), per scope: packs of consecutive vertices of degree
@@ -233,27 +244,23 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             }
             for (auto &x : th) x.join();
         }
-        int64_t toff = 0, ooff = 0;
+        int64_t ooff = 0;
         for (int32_t v : big) {
             const int64_t deg = off[v + 1] - off[v];
             const int32_t b = (int32_t)S.big_v.size();
             S.big_v.push_back(v);
-            S.big_c0.push_back((int32_t)S.chunk_big.size());
-            const uint32_t cap = hub_table_slots(deg, kHubSlotsPerEdge);
-            S.big_toff.push_back(toff);
-            S.big_tcap.push_back(cap);
+            S.big_deg.push_back(deg);
             S.big_ooff.push_back(ooff);
             for (int64_t e = off[v]; e < off[v + 1]; e += kBigChunk) {
                 S.chunk_big.push_back(b);
                 S.chunk_e0.push_back(e);
                 S.chunk_e1.push_back(std::min<int64_t>(e + kBigChunk, off[v + 1]));
             }
-            for (int64_t i = 0; i < deg; i += kBigSlotChunk) {  // over the occupied list
+            for (int64_t i = 0; i < deg; i += kBigSlotChunk) {  // over the distinct list
                 S.schunk_big.push_back(b);
                 S.schunk_s0.push_back(i);
                 S.schunk_s1.push_back(std::min<int64_t>(i + kBigSlotChunk, deg));
             }
-            toff += cap;
             ooff += deg;
             S.m_big += deg;
         }
@@ -261,9 +268,7 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         sc.nb = (int32_t)S.big_v.size() - sc.b0;
         sc.nc = (int32_t)S.chunk_big.size() - sc.c0;
         sc.ns = (int32_t)S.schunk_big.size() - sc.s0;
-        sc.table_slots = toff;
         sc.occ_slots = ooff;
-        S.max_table_slots = std::max(S.max_table_slots, toff);
         S.max_occ_slots = std::max(S.max_occ_slots, ooff);
         S.max_scope_edges = std::max(S.max_scope_edges, sc.e1 - sc.e0);
         S.max_scope_small = std::max(S.max_scope_small, nsmall);
@@ -271,7 +276,7 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         S.max_scope_vertices = std::max(S.max_scope_vertices, sc.v1 - sc.v0);
         S.scopes.push_back(sc);
     }
-    S.big_c0.push_back((int32_t)S.chunk_big.size());
+    plan_hub_parts(S, 0);
     return true;
 }
 
@@ -358,14 +363,6 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
         GALP_CUDA(cudaStreamSynchronize(st));  // the copies read the caller's buffers
         return brc != GALP_OK ? brc : GALP_EFORMAT;
     }
-    {
-        // hub tables at 2 slots per edge when 4 would take more than a third of the free
-        // device memory (very hub-heavy graphs)
-        size_t free_b = 0, total_b = 0;
-        GALP_CUDA(cudaMemGetInfo(&free_b, &total_b));
-        if ((double)sizeof(unsigned long long) * (double)sched.max_table_slots > (double)free_b / 3)
-            resize_hub_tables(sched, g.offsets, 2);
-    }
     phase(0);
 
     if (policy != 0) {
@@ -391,8 +388,6 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     if ((rc = upload(b_pack_nv, d_pack_nv, sched.pack_nv, st, h2d))) return rc;
     if ((rc = upload(b_mid_v, d_mid_v, sched.mid_v, st, h2d))) return rc;
     if ((rc = upload(b_big_v, d_big_v, sched.big_v, st, h2d))) return rc;
-    if ((rc = upload(b_big_toff, d_big_toff, sched.big_toff, st, h2d))) return rc;
-    if ((rc = upload(b_big_tcap, d_big_tcap, sched.big_tcap, st, h2d))) return rc;
     if ((rc = upload(b_big_ooff, d_big_ooff, sched.big_ooff, st, h2d))) return rc;
     if ((rc = upload(b_chunk_big, d_chunk_big, sched.chunk_big, st, h2d))) return rc;
     if ((rc = upload(b_chunk_e0, d_chunk_e0, sched.chunk_e0, st, h2d))) return rc;
@@ -400,8 +395,7 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     if ((rc = upload(b_schunk_big, d_schunk_big, sched.schunk_big, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s0, d_schunk_s0, sched.schunk_s0, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s1, d_schunk_s1, sched.schunk_s1, st, h2d))) return rc;
-    if ((rc = upload(b_big_c0, d_big_c0, sched.big_c0, st, h2d))) return rc;
-    GALP_CUDA(b_bpart.alloc(sizeof(int) * 4 * std::max<size_t>(sched.chunk_big.size(), 1)));
+    if ((rc = setup_hub_parts(0, st, h2d))) return rc;
     // per-vertex state, spill and tied lists
     const size_t nn = (size_t)std::max<int64_t>(n, 1);
     GALP_CUDA(b_dcnt.alloc(sizeof(int32_t) * nn));
@@ -444,22 +438,7 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     const size_t nbig = sched.big_v.size();
     GALP_CUDA(b_bstat.alloc(sizeof(BigStat) * std::max<size_t>(nbig, 1)));
     GALP_CUDA(b_big_a.alloc(sizeof(int64_t) * std::max<size_t>(nbig, 1)));
-    GALP_CUDA(b_gtab.alloc(sizeof(unsigned long long) * std::max<int64_t>(sched.max_table_slots, 1)));
-    GALP_CUDA(b_occ.alloc(sizeof(uint32_t) * std::max<int64_t>(sched.max_occ_slots, 1)));
-    if (sched.max_table_slots) {
-        GALP_CUDA(cudaMemsetAsync(b_gtab.p, 0, sizeof(unsigned long long) * sched.max_table_slots, st));
-        // slot layout: generation | label | count, counts up to the largest hub degree
-        int64_t maxdeg = 1;
-        for (int32_t v : sched.big_v) maxdeg = std::max<int64_t>(maxdeg, g.offsets[v + 1] - g.offsets[v]);
-        int cb = 1, lb = 1;
-        while (cb < 31 && (maxdeg >> cb)) ++cb;
-        while (lb < 31 && ((std::max<int64_t>(n, 2) - 1) >> lb)) ++lb;
-        hub_cbits = cb;
-        hub_gshift = cb + lb;
-        hub_lmask = lb >= 32 ? 0xFFFFFFFFu : ((1u << lb) - 1u);
-        hub_gen_max = (uint32_t)std::min<int64_t>(((int64_t)1 << std::min(64 - cb - lb, 31)) - 1, 0x7FFFFFFF);
-        hub_gen = 0;
-    }
+    GALP_CUDA(b_big_list.alloc(sizeof(unsigned long long) * std::max<int64_t>(sched.max_occ_slots, 1)));
     if (nbig) {
         init_bigstat_kernel<<<(unsigned)((nbig + 255) / 256), 256, 0, st>>>((BigStat *)b_bstat.p, (int)nbig);
         GALP_CUDA(cudaGetLastError());
@@ -557,6 +536,30 @@ int Engine::setup_batch(const galp_csr &g, const int64_t *graph_v0, int32_t coun
     return bad ? GALP_EFORMAT : GALP_OK;
 }
 
+int Engine::setup_hub_parts(int shift, cudaStream_t st, int64_t &h2d)
+{
+    plan_hub_parts(sched, shift);
+    int rc;
+    if ((rc = upload(b_hub_p0, d_hub_p0, sched.hub_p0, st, h2d))) return rc;
+    if ((rc = upload(b_hub_pbase, d_hub_pbase, sched.hub_pbase, st, h2d))) return rc;
+    if ((rc = upload(b_hub_pcap, d_hub_pcap, sched.hub_pcap, st, h2d))) return rc;
+    if ((rc = upload(b_part_big, d_part_big, sched.part_big, st, h2d))) return rc;
+    const size_t nparts = std::max<size_t>(sched.part_big.size(), 1);
+    GALP_CUDA(b_pfill.alloc(sizeof(int) * nparts));
+    GALP_CUDA(cudaMemsetAsync(b_pfill.p, 0, sizeof(int) * nparts, st));
+    GALP_CUDA(b_psum.alloc(sizeof(int4) * nparts));
+    GALP_CUDA(b_pairs.alloc(sizeof(unsigned long long) * (size_t)std::max<int64_t>(sched.max_pair_slots, 1)));
+    if (!hub_count_blocks && !sched.part_big.empty()) {
+        const int smem = (int)(sizeof(uint32_t) * 2 * kHubTab);
+        GALP_CUDA(cudaFuncSetAttribute(hub_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        int occ = 0;
+        GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hub_count_kernel, kTB, smem));
+        hub_count_blocks = std::max(occ, 1) * sms;
+    }
+    GALP_CUDA(cudaStreamSynchronize(st));
+    return GALP_OK;
+}
+
 IterArgs Engine::big_args(const Scope &sc) const
 {
     IterArgs a{};
@@ -566,8 +569,6 @@ IterArgs Engine::big_args(const Scope &sc) const
     a.b0 = sc.b0;
     a.nbig = sc.nb;
     a.big_v = d_big_v;
-    a.big_toff = d_big_toff;
-    a.big_tcap = d_big_tcap;
     a.big_ooff = d_big_ooff;
     a.c0 = sc.c0;
     a.chunk_big = d_chunk_big;
@@ -578,17 +579,19 @@ IterArgs Engine::big_args(const Scope &sc) const
     a.schunk_big = d_schunk_big;
     a.schunk_s0 = d_schunk_s0;
     a.schunk_s1 = d_schunk_s1;
-    a.big_c0 = d_big_c0;
-    a.bpart = (int *)b_bpart.p;
     a.nschunks = sc.ns;
-    a.gtab = (unsigned long long *)b_gtab.p;
-    a.hub_gen = hub_gen;
-    a.hub_cbits = hub_cbits;
-    a.hub_gshift = hub_gshift;
-    a.hub_lmask = hub_lmask;
+    a.hub_p0 = d_hub_p0;
+    a.hub_pbase = d_hub_pbase;
+    a.hub_pcap = d_hub_pcap;
+    a.part_big = d_part_big;
+    a.q0 = sc.q0;
+    a.nparts = sc.nq;
+    a.pfill = (int *)b_pfill.p;
+    a.psum = (int4 *)b_psum.p;
+    a.pairs = (unsigned long long *)b_pairs.p;
+    a.big_list = (unsigned long long *)b_big_list.p;
     a.bstat = (BigStat *)b_bstat.p;
     a.big_a = (int64_t *)b_big_a.p;
-    a.big_occ = (uint32_t *)b_occ.p;
     a.runbase = (const int64_t *)b_runbase.p;
     a.nbr_shift = (policy == 0) ? 0 : sc.e0;
     return a;
@@ -690,12 +693,6 @@ int Engine::launch_limits()
 int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, const int32_t *lab_in,
                           int32_t *lab_out, const uint8_t *dirty, int32_t *changed)
 {
-    if (sc.nb) {  // a new generation for the hub tables: the previous scope's slots turn free
-        if (++hub_gen > hub_gen_max) {
-            GALP_CUDA(cudaMemsetAsync(b_gtab.p, 0, b_gtab.bytes, st));
-            hub_gen = 1;
-        }
-    }
     if (!occ_mid) {
         int rc = launch_limits();
         if (rc) return rc;
@@ -719,6 +716,8 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         if (prof.on) e0 = prof.mark(st);
         big_insert_kernel<<<a.nchunks, kTB, 0, st>>>(a);
         launched("big_insert_kernel", st);
+        hub_count_kernel<<<std::min(a.nparts, hub_count_blocks), kTB, sizeof(uint32_t) * 2 * kHubTab, st>>>(a);
+        launched("hub_count_kernel", st);
         big_combine_kernel<<<(a.nbig + 7) / 8, 256, 0, st>>>(a);
         launched("big_combine_kernel", st);
         big_stats_kernel<<<a.nschunks, kTB, 0, st>>>(a);
@@ -911,7 +910,8 @@ int Engine::enqueue_run_incore(cudaStream_t st, int niter, long long thr)
 // batches in order, each gathering from the current labels (earlier batches of the
 // iteration already applied) and committing its own labels when it is done.  Policy 2
 // copies batch j+1 on the copy stream while batch j computes; events order buffer
-// reuse.  The host waits once per iteration, for the early-exit decision.
+// reuse.  With early exit on, the host waits once per iteration for the decision; with
+// it off, the whole run is enqueued without a wait.
 int Engine::run_outofcore(cudaStream_t st, int niter, long long thr)
 {
     int32_t *cur = (int32_t *)b_lab0.p, *tmp = (int32_t *)b_lab1.p;
@@ -964,10 +964,16 @@ int Engine::run_outofcore(cudaStream_t st, int niter, long long thr)
         finalize_kernel<<<1, 1, 0, st>>>((Ctl *)b_ctl.p);
         launched("finalize_kernel", st);
         GALP_CUDA(cudaGetLastError());
-        int active = 0;
-        GALP_CUDA(cudaMemcpyAsync(&active, &((Ctl *)b_ctl.p)->active, sizeof(int), cudaMemcpyDeviceToHost, st));
-        GALP_CUDA(cudaStreamSynchronize(st));
-        if (!active) break;
+        // Without early exit every iteration runs: nothing to wait for, the copy stream
+        // keeps streaming the next iteration's batches.  With it, the host reads the
+        // device's decision once per iteration (the next iteration's first batch is
+        // already being copied meanwhile), so no batch is streamed after the exit.
+        if (thr >= 0 && it + 1 < niter) {
+            int active = 0;
+            GALP_CUDA(cudaMemcpyAsync(&active, &((Ctl *)b_ctl.p)->active, sizeof(int), cudaMemcpyDeviceToHost, st));
+            GALP_CUDA(cudaStreamSynchronize(st));
+            if (!active) break;
+        }
     }
     if (copy_stream) GALP_CUDA(cudaStreamSynchronize(copy_stream));
     return GALP_OK;
@@ -1118,6 +1124,7 @@ int galp_enqueue(galp_ctx *ctx, int32_t niter)
     if (rc) return rc;
     GALP_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     ctx->pending = true;
+    ctx->last_niter = niter;
     return GALP_OK;
 }
 
@@ -1127,6 +1134,16 @@ int galp_sync(galp_ctx *ctx, galp_stats *st)
     GALP_CUDA(cudaStreamSynchronize(ctx->stream));
     Ctl c;
     GALP_CUDA(cudaMemcpy(&c, ctx->eng.b_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    // a hub partition overflowed (its pairs were dropped): redo the run with twice the
+    // partitions, up to 64x the default count (the labels of the redone run are exact)
+    while ((c.err & kErrHubOverflow) && ctx->eng.sched.hub_shift < kMaxHubShift) {
+        int64_t h2d = 0;
+        int rc = ctx->eng.setup_hub_parts(ctx->eng.sched.hub_shift + 1, ctx->stream, h2d);
+        if (rc) return rc;
+        if ((rc = galp_enqueue(ctx, ctx->last_niter))) return rc;
+        GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+        GALP_CUDA(cudaMemcpy(&c, ctx->eng.b_ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost));
+    }
     ctx->iters = c.iter;
     ctx->err = c.err;
     ctx->runs_last = c.N;
@@ -1144,6 +1161,7 @@ int galp_sync(galp_ctx *ctx, galp_stats *st)
         for (int i = 0; i < GALP_MAX_ITERS; ++i) st->updates[i] = (int64_t)c.counts[i];
     }
     if (c.err & kErrFormat) return GALP_EFORMAT;
+    if (c.err & kErrHubOverflow) return GALP_ENOMEM;
     return (c.err & kErrLookback) ? GALP_ETIMEOUT : GALP_OK;
 }
 
@@ -1215,7 +1233,7 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
     info->nmid = nms;
     info->nlarge = nml;
     info->nbig = (int64_t)E.sched.big_v.size();
-    info->table_slots = E.sched.max_table_slots;
+    info->table_slots = E.sched.max_pair_slots;
     info->launches_per_iter = 14 + (info->nbig ? 7 : 0) + (E.frontier ? 1 : 0);
     info->flags = (E.adj_sorted ? GALP_SCHED_SORTED : 0) | (E.symmetric ? GALP_SCHED_SYMMETRIC : 0) |
                   (E.frontier ? GALP_SCHED_FRONTIER : 0);
@@ -1229,6 +1247,13 @@ int galp_set_variant(galp_ctx *ctx, const galp_variant *v)
     if (!ctx || !v || v->agg_mode < 0 || v->agg_mode > 2 || !(v->frontier_frac >= 0.f && v->frontier_frac <= 1.f) ||
         !(v->learned_margin >= 0.f && v->learned_margin < 10.f) || v->small_sort < 0 || v->small_sort > 1)
         return GALP_EINVAL;
+    if (v->hub_part_shift < -16 || v->hub_part_shift > kMaxHubShift) return GALP_EINVAL;
+    if (v->hub_part_shift != ctx->eng.sched.hub_shift) {
+        int64_t h2d = 0;
+        GALP_CUDA(cudaStreamSynchronize(ctx->stream));
+        const int rc = ctx->eng.setup_hub_parts(v->hub_part_shift, ctx->stream, h2d);
+        if (rc) return rc;
+    }
     ctx->eng.variant = *v;
     return GALP_OK;
 }
@@ -1237,6 +1262,7 @@ int galp_get_variant(galp_ctx *ctx, galp_variant *v)
 {
     if (!ctx || !v) return GALP_EINVAL;
     *v = ctx->eng.variant;
+    v->hub_part_shift = ctx->eng.sched.hub_shift;
     return GALP_OK;
 }
 

@@ -54,8 +54,9 @@ struct Scope {
     int32_t c0 = 0, nc = 0;    // big insert chunks
     int32_t s0 = 0, ns = 0;    // big stats chunks
     int32_t last_v = -1;       // last vertex of the scope that owns runs
-    int64_t table_slots = 0;   // global-table slots of the scope's big vertices
-    int64_t occ_slots = 0;     // occupied-list capacity of the scope's big vertices
+    int32_t q0 = 0, nq = 0;    // hash partitions of the scope's big vertices
+    int64_t pair_slots = 0;    // pair area of those partitions
+    int64_t occ_slots = 0;     // distinct-list capacity of the scope's big vertices
 };
 
 // Static schedule of a graph (host side, built once): degree buckets per scope.
@@ -65,16 +66,20 @@ struct Schedule {
     std::vector<int32_t> mid_v;      // per scope: mid, large and xl vertices in ascending degree
     std::vector<int32_t> mid_deg;    // degree of each mid_v entry
     std::vector<int32_t> big_v;      // vertex of each big entry
-    std::vector<int64_t> big_toff;   // table offset, relative to its scope
-    std::vector<uint32_t> big_tcap;  // table capacity (4 slots per edge; 2 when device memory is short)
-    std::vector<int64_t> big_ooff;   // occupied-list offset, relative to its scope
+    std::vector<int64_t> big_deg;    // its degree
+    std::vector<int64_t> big_ooff;   // distinct-list offset, relative to its scope
     std::vector<int32_t> chunk_big;
     std::vector<int64_t> chunk_e0, chunk_e1;
     std::vector<int32_t> schunk_big;
-    std::vector<int32_t> big_c0;     // first insert chunk of each big vertex, then the total
     std::vector<int64_t> schunk_s0, schunk_s1;
+    // hash partitions of the big vertices' (label, count) pairs (plan_hub_parts)
+    std::vector<int32_t> hub_p0;     // first partition of each big vertex, then the total
+    std::vector<int64_t> hub_pbase;  // pair-area offset of its partitions, relative to its scope
+    std::vector<int32_t> hub_pcap;   // pair capacity of each of its partitions
+    std::vector<int32_t> part_big;   // big vertex of each partition
+    int hub_shift = 0;               // partitions per hub: degree * 2^hub_shift / kHubPartPairs
     std::vector<Scope> scopes;
-    int64_t max_table_slots = 0, max_occ_slots = 0, max_scope_edges = 0, m_big = 0;
+    int64_t max_pair_slots = 0, max_occ_slots = 0, max_scope_edges = 0, m_big = 0;
     int64_t max_scope_small = 0, max_scope_mid = 0, max_scope_vertices = 0;
     double deg_hist[kDegBins] = {};  // CSR entries by log2 degree (dispatch features)
 };
@@ -82,6 +87,11 @@ struct Schedule {
 // Build the schedule; scope_starts = first vertex of every scope, then n.  False when
 // the offsets decrease somewhere.
 bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts);
+
+// (Re)plan the hash partitions of every big vertex: degree * 2^shift / kHubPartPairs
+// partitions (at least one), each holding 1.5x its share of the degree plus 256 pairs,
+// at most kHubPartCap.
+void plan_hub_parts(Schedule &S, int shift);
 
 // Batch boundaries of OutOfCore::compute_batch_boundaries (outofcore.cuh:38-60) for
 // 2^buffer_pow edges; returns GALP_EBATCH where the reference would loop forever.
@@ -175,9 +185,10 @@ struct Engine {
     const int32_t *h_nbr = nullptr;  // caller's host neighbours (streamed for policies 1/2)
     bool registered = false;         // the library pinned h_nbr
     Schedule sched;
-    DevBuf b_nbr[2], b_off, b_pack_v0, b_pack_nv, b_mid_v, b_big_v, b_big_toff, b_big_tcap;
-    DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff, b_big_c0, b_bpart;
-    DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_gtab, b_occ, b_bad;
+    DevBuf b_nbr[2], b_off, b_pack_v0, b_pack_nv, b_mid_v, b_big_v;
+    DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff;
+    DevBuf b_hub_p0, b_hub_pbase, b_hub_pcap, b_part_big, b_pfill, b_psum, b_pairs, b_big_list;
+    DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_bad;
     DevBuf b_dcnt, b_runbase, b_c0, b_c1, b_kw, b_r, b_run_lab, b_run_cnt, b_tsmall, b_tmid, b_bsum;
     DevBuf b_dirty, b_changed, b_chk;  // frontier mode; setup adjacency checks
     DevBuf b_static_feat, b_vtab, b_disp, b_feat_log, b_var_log, b_weights;  // dispatch
@@ -191,27 +202,25 @@ struct Engine {
     uint8_t *d_pack_nv = nullptr;
     int32_t *d_mid_v = nullptr;
     int32_t *d_big_v = nullptr;
-    int64_t *d_big_toff = nullptr, *d_big_ooff = nullptr;
-    uint32_t *d_big_tcap = nullptr;
+    int64_t *d_big_ooff = nullptr;
     int32_t *d_chunk_big = nullptr;
     int64_t *d_chunk_e0 = nullptr, *d_chunk_e1 = nullptr;
     int32_t *d_schunk_big = nullptr;
     int64_t *d_schunk_s0 = nullptr, *d_schunk_s1 = nullptr;
-    int32_t *d_big_c0 = nullptr;
+    int32_t *d_hub_p0 = nullptr, *d_hub_pcap = nullptr, *d_part_big = nullptr;
+    int64_t *d_hub_pbase = nullptr;
     int sms = 1;
     bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
     bool symmetric = false;   // edge multiset symmetric (frontier marking along out-edges)
     Profiler prof;
-    galp_variant variant{0, 0.05f, 0.03f, 0, {}};  // kernel variant knobs (galp_set_variant)
+    galp_variant variant{0, 0.05f, 0.03f, 0, 0, {}};  // kernel variant knobs (galp_set_variant)
     // out-of-core streaming
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
     uint64_t batch_seq = 0;   // running batch counter (buffer parity)
     int64_t h2d_run = 0;      // bytes streamed by the last run
     int64_t launches = 0;     // kernels launched by runs so far (setup excluded)
-    // hub tables: generation of the scope being enqueued, slot layout
-    uint32_t hub_gen = 0, hub_gen_max = 1, hub_lmask = 0;
-    int hub_cbits = 1, hub_gshift = 2;
+    int hub_count_blocks = 0; // resident blocks of hub_count_kernel (grid = one wave)
     double setup_ms[5] = {};  // host schedule, CSR upload, state upload, dispatch prep, device checks
     // batched mode: graph g = vertices [g_v0[g], g_v0[g+1]) of the concatenated CSR
     bool batched = false;
@@ -229,6 +238,8 @@ struct Engine {
     // would start its blocks' whole shares late
     int occ_mid = 0, occ_resolve = 0, occ_resolve_mid = 0;
     int launch_limits();
+    // hub partitions at 2^shift times the default count: plan, upload, size the pair area
+    int setup_hub_parts(int shift, cudaStream_t st, int64_t &h2d);
     int setup_batch(const galp_csr &g, const int64_t *graph_v0, int32_t count, const galp_opts &o, cudaStream_t st,
                     int64_t &h2d);
     void launched(const char *name, cudaStream_t st)
@@ -259,6 +270,7 @@ struct galp_ctx {
     // batched mode: the whole run captured once per iteration count as a CUDA graph
     cudaGraphExec_t graph_exec = nullptr;
     int graph_iters = -1;
+    int last_niter = 0;      // iterations of the last enqueued run (redone after a hub overflow)
     int64_t n = 0, m = 0;
     cudaStream_t own_stream = nullptr;
     cudaStream_t stream = nullptr;

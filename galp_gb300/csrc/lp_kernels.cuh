@@ -34,7 +34,10 @@ constexpr int kTileSlots = 2048;      // shared-memory label slots per tile
 constexpr int kTileV = 512;           // vertices per tile
 constexpr int kSmallMax = 32;         // degree handled by one warp pack
 constexpr int kBigChunk = 1024;       // edges per big_insert CTA
-constexpr int kBigSlotChunk = 8192;   // occupied-list entries per big_stats CTA
+constexpr int kBigSlotChunk = 8192;   // distinct-list entries per big_stats CTA
+constexpr int kHubPartPairs = 2048;   // target pairs per hub partition (a hub of degree D: D / 2048 partitions)
+constexpr int kHubPartCap = 4096;     // largest pair capacity of a partition (its table has 2x the slots)
+constexpr int kHubTab = 2 * kHubPartCap;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
 constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound (about a second)
@@ -42,6 +45,8 @@ constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound 
 // error bits in Ctl::err
 constexpr int kErrLookback = 1;
 constexpr int kErrFormat = 2;
+constexpr int kErrHubOverflow = 4;  // a hub partition received more pairs than it holds (the run is redone
+                                    // with twice the partitions)
 
 struct Ctl {
     int active;                 // 1 while iterations still run
@@ -95,31 +100,31 @@ struct IterArgs {
     unsigned wait_xor;          // look-back accepts statuses of epoch ^ wait_xor (0; tests only)
     long long spin_limit;       // look-back polls before a wait gives up
     Ctl *ctl;
-    // big vertices
+    // big vertices (hubs): each hub's labels are counted by hash partitions of its
+    // distinct (label, count) pairs, one shared-memory table per partition
     int32_t nbig;
     const int32_t *big_v;       // vertex of each big entry
-    const int64_t *big_toff;    // table offset of each big entry
-    const uint32_t *big_tcap;   // table capacity (4 or 2 slots per edge, a multiple of 4)
     const int32_t *chunk_big;   // insert chunk -> big index
     const int64_t *chunk_e0;    // insert chunk -> first edge
     const int64_t *chunk_e1;    // insert chunk -> end edge
     int32_t nchunks;
     const int32_t *schunk_big;  // stats chunk -> big index
-    const int64_t *schunk_s0;   // stats chunk -> first entry of the vertex's occupied list
+    const int64_t *schunk_s0;   // stats chunk -> first entry of the vertex's distinct list
     const int64_t *schunk_s1;
     int32_t nschunks;
-    unsigned long long *gtab;   // big tables: 64-bit slots generation | label | count
-    uint32_t hub_gen;           // generation of this scope's tables (slots of others are free)
-    int32_t hub_cbits;          // count bits (counts <= the largest hub degree)
-    int32_t hub_gshift;         // generation shift = count bits + label bits
-    uint32_t hub_lmask;         // label mask after the count shift
+    const int32_t *hub_p0;      // first partition of each big vertex (global index; nbig + 1 entries)
+    const int64_t *hub_pbase;   // pair-area offset of each big vertex's partitions (scope-relative)
+    const int32_t *hub_pcap;    // pair capacity of each partition of the big vertex
+    const int32_t *part_big;    // partition -> big index
+    int32_t q0, nparts;         // the scope's partitions
+    int *pfill;                 // pairs appended to each partition (hub_count_kernel resets it)
+    int4 *psum;                 // per partition: max count, candidates, smallest, largest
+    unsigned long long *pairs;  // pair area: label << 32 | count
+    unsigned long long *big_list;  // distinct label << 32 | count of each big vertex (capacity = degree)
+    const int64_t *big_ooff;    // offset of each big vertex's distinct list (scope-relative)
     BigStat *bstat;
     int64_t *big_a;             // run base of each big vertex (written by the scan)
-    uint32_t *big_occ;          // occupied-slot list of each big table (capacity = degree)
-    const int64_t *big_ooff;    // offset of each big vertex's occupied list
     const int64_t *runbase;     // run base of every vertex when the scan precedes big_resolve
-    int *bpart;                 // per insert chunk: max count, candidates, smallest, largest
-    const int32_t *big_c0;      // first insert chunk of each big vertex (nbig + 1 entries)
     int32_t *changed;           // frontier mode: vertices whose label changes (else null)
 };
 
@@ -297,22 +302,13 @@ struct RunListQuery {
 struct SplitTable {  // separate key and count arrays (shared-memory regions)
     const uint32_t *key;
     const uint32_t *cnt;
-    __device__ static uint32_t start(uint32_t k, uint32_t cap) { return hslot(k, cap); }
     __device__ uint32_t k(int s) const { return key[s]; }
     __device__ uint32_t c(int s) const { return cnt[s]; }
 };
-struct HubTable {  // generation-tagged 64-bit slots (global hub tables)
-    const unsigned long long *tab;
-    int cbits, gshift;
-    uint32_t lmask, gen;
-    // probing starts at the 4-slot (32-byte) group of the hash slot
-    __device__ static uint32_t start(uint32_t k, uint32_t cap) { return hslot(k, cap) & ~3u; }
-    __device__ uint32_t k(int s) const
-    {
-        const unsigned long long x = tab[s];
-        return (uint32_t)(x >> gshift) == gen ? (uint32_t)(x >> cbits) & lmask : kEmpty;
-    }
-    __device__ uint32_t c(int s) const { return (uint32_t)(tab[s] & ((1ull << cbits) - 1)); }
+struct DenseTable {  // a big vertex's distinct list: label << 32 | count, every entry occupied
+    const unsigned long long *list;
+    __device__ uint32_t k(int s) const { return (uint32_t)(list[s] >> 32); }
+    __device__ uint32_t c(int s) const { return (uint32_t)list[s]; }
 };
 
 // Open-addressed table region of one vertex, scanned by one warp.
@@ -325,11 +321,9 @@ struct WarpTableQueryT {
     int *hist;
     int lane;
     uint32_t *scratch;  // kPickScratch entries for tile_pick (only vertices with >= kTile distinct labels)
-    const uint32_t *occ = nullptr;  // optional list of the occupied slots (global tables)
-    int nocc = 0;
 
-    __device__ int nslots() const { return occ ? nocc : cap; }
-    __device__ int slot(int i) const { return occ ? (int)occ[i] : i; }
+    __device__ int nslots() const { return cap; }
+    __device__ int slot(int i) const { return i; }
 
     // x-th smallest key (0-based) among the occupied slots
     __device__ uint32_t select(int x)
@@ -421,19 +415,9 @@ struct WarpTableQueryT {
         if (best < 0) return -1;
         return rank_of((uint32_t)best);
     }
-    __device__ uint32_t count_of(uint32_t k) const
-    {
-        uint32_t h = T::start(k, (uint32_t)cap);
-        for (int probes = 0; probes < cap; ++probes) {
-            const uint32_t x = t.k((int)h);
-            if (x == k) return t.c((int)h);
-            if (x == kEmpty) return 0;
-            h = (h + 1 == (uint32_t)cap) ? 0 : h + 1;
-        }
-        return 0;
-    }
     // Sort the tile's kTile distinct labels (ranks [lo, lo + kTile)) in scratch and
-    // pick the candidate of highest tile_priority.
+    // pick the candidate of highest tile_priority.  Entries are label << 1 | candidate
+    // (labels are below 2^31 - 1, so they sort by label and stay below kEmpty).
     __device__ int tile_pick(int64_t lo)
     {
         if (!scratch) return -1;
@@ -442,11 +426,12 @@ struct WarpTableQueryT {
         int base = 0;
         for (int i0 = 0; i0 < nslots(); i0 += 32) {
             const int i = i0 + lane;
-            const uint32_t k = (i < nslots()) ? t.k(slot(i)) : kEmpty;
+            const int s = (i < nslots()) ? slot(i) : 0;
+            const uint32_t k = (i < nslots()) ? t.k(s) : kEmpty;
             const bool in = k != kEmpty && k >= Llo && k < Lhi;
             const unsigned m = __ballot_sync(kFull, in);
             if (in && base + __popc(m & ((1u << lane) - 1)) < kPickScratch)
-                scratch[base + __popc(m & ((1u << lane) - 1))] = k;
+                scratch[base + __popc(m & ((1u << lane) - 1))] = (k << 1) | ((int)t.c(s) == W ? 1u : 0u);
             base += __popc(m);
         }
         const int nin = min(base, kPickScratch);
@@ -470,7 +455,7 @@ struct WarpTableQueryT {
         }
         int best = -1, bi = -1;
         for (int i = lane; i < nin; i += 32) {
-            if ((int)count_of(scratch[i]) == W && tile_priority(i) > best) {
+            if ((scratch[i] & 1u) && tile_priority(i) > best) {
                 best = tile_priority(i);
                 bi = i;
             }
@@ -896,15 +881,24 @@ __global__ void __launch_bounds__(kTB, 3) lp_tile_kernel(IterArgs p)
 // big vertices
 // ---------------------------------------------------------------------------
 
-// Count the labels of one chunk of a big vertex's edges in shared memory, then merge
-// the distinct (label, count) pairs into the vertex's global table.
-__global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
+// Partition of a hub's label: the high bits of a hash independent of the one that places
+// labels in a partition's table (hslot).
+__device__ __forceinline__ uint32_t hub_part(uint32_t label, uint32_t nparts)
+{
+    return __umulhi(mix32(label ^ 0x9E3779B9u), nparts);
+}
+
+// Count the labels of one chunk of a big vertex's edges in shared memory, then append
+// the chunk's distinct (label, count) pairs to the vertex's hash partitions (one
+// reservation per warp and partition; appends to a partition are contiguous, so its
+// sectors fill in L2).  A partition that is full drops the pair and flags the run, which
+// the host then redoes with twice the partitions.
+__global__ void __launch_bounds__(kTB, 8) big_insert_kernel(IterArgs p)
 {
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
     __shared__ uint16_t sused[kBigChunk];     // occupied local slots, compacted
-    __shared__ uint32_t screated[kBigChunk];  // global slots this chunk claimed
-    __shared__ int nused, ncreated, obase;
+    __shared__ int nused;
     if (!ctl_active(p.ctl)) return;
     if ((int)blockIdx.x >= p.nchunks) return;
     const int ch = p.c0 + blockIdx.x;
@@ -915,7 +909,7 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
         skey[s] = kEmpty;
         scnt[s] = 0;
     }
-    if (threadIdx.x == 0) nused = ncreated = 0;
+    if (threadIdx.x == 0) nused = 0;
     __syncthreads();
     {
         // all of a thread's neighbour loads, then all its label gathers, in flight together
@@ -946,8 +940,8 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
         }
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // compact the occupied local slots, so the merge rounds below run on full warps
+    const int lane = threadIdx.x & 31;
+    // compact the occupied local slots, so the append rounds below run on full warps
     for (int s0 = 0; s0 < (int)cap; s0 += kTB) {
         const int s = s0 + threadIdx.x;
         const bool used = skey[s] != kEmpty;
@@ -960,132 +954,36 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
     }
     __syncthreads();
     const int nloc = nused;
-    // Merge into the vertex's global table of generation-tagged 64-bit slots: a slot of
-    // another generation is free, so tables are never cleared between iterations.  The
-    // count is the low field; a 32-bit add on the slot's low word never carries into the
-    // label (a count stays below 2^hub_cbits).  Every merge observes the label's count
-    // right after it (the claim: its own count; an add: the returned old count plus its
-    // own); the last merge of a label observes its final count, so the observations fold
-    // into the vertex's maximum count, candidates and their extreme labels
-    // (big_combine_kernel folds the chunks) without a pass over the table.
-    const int64_t toff = p.big_toff[bi];
-    const uint32_t gcap = p.big_tcap[bi];
-    unsigned long long *gt = p.gtab + toff;
-    uint32_t *occ = p.big_occ + p.big_ooff[bi];
-    int *dcount = &p.bstat[bi].d;
-    const uint32_t gen = p.hub_gen;
-    const uint32_t cmask = (1u << p.hub_cbits) - 1u;  // hub_cbits <= 31
-    int oW = 0, ok = 0, omn = INT_MAX, omx = -1;      // observations of this thread
-    auto observe = [&](uint32_t L, uint32_t now) {
-        const int x = (int)now;
-        if (x > oW) {
-            oW = x;
-            ok = 1;
-            omn = omx = (int)L;
-        } else if (x == oW) {
-            ok++;
-            omn = min(omn, (int)L);
-            omx = max(omx, (int)L);
-        }
-    };
-    // Probing walks 4-slot groups (one 32-byte sector, read with two 16-byte loads in
-    // flight together) from the group of the hash slot: the same slot order as linear
-    // probing from the group's first slot, with one memory round trip per group.
+    const int q = p.hub_p0[bi];
+    const uint32_t np = (uint32_t)(p.hub_p0[bi + 1] - q);
+    const int pcap = p.hub_pcap[bi];
+    unsigned long long *area = p.pairs + p.hub_pbase[bi];
     for (int base = 0; base < nloc; base += kTB) {  // block-uniform trip count
         const int i = base + threadIdx.x;
-        bool created = false;
-        uint32_t g = 0, j = 0;
+        uint32_t L = kEmpty, c = 0;
+        int part = -1;
         if (i < nloc) {
-            const uint32_t ls = sused[i], L = skey[ls], c = scnt[ls];
-            const unsigned long long tag = ((unsigned long long)gen << p.hub_gshift) |
-                                           ((unsigned long long)L << p.hub_cbits);
-            const unsigned long long key = tag >> p.hub_cbits;
-            g = hslot(L, gcap) & ~3u;
-            for (;;) {
-                unsigned long long x[4];
-                ld_relaxed_group4(&gt[g], x);
-                bool done = false;
-#pragma unroll
-                for (int jj = 0; jj < 4; ++jj) {
-                    if (done) break;
-                    unsigned long long xv = x[jj];
-                    for (;;) {
-                        if ((xv >> p.hub_cbits) == key) {  // same generation and label
-                            observe(L, (atomicAdd((unsigned int *)&gt[g + jj], c) & cmask) + c);
-                            done = true;
-                            break;
-                        }
-                        if ((uint32_t)(xv >> p.hub_gshift) != gen) {  // free: claim it
-                            const unsigned long long pv = atomicCAS(&gt[g + jj], xv, tag | c);
-                            if (pv == xv) {
-                                observe(L, c);
-                                created = done = true;
-                                break;
-                            }
-                            xv = pv;  // taken meanwhile: look at it again
-                            continue;
-                        }
-                        break;  // another label's slot: the next one
-                    }
-                    if (done) j = (uint32_t)jj;
-                }
-                if (done) break;
-                g = (g + 4 == gcap) ? 0 : g + 4;  // gcap is a multiple of 4
-            }
+            const uint32_t ls = sused[i];
+            L = skey[ls];
+            c = scnt[ls];
+            part = (int)hub_part(L, np);
         }
-        // collect the claimed slots (warp-aggregated) for the vertex's occupied list
-        const unsigned m = __ballot_sync(kFull, created);
-        if (m) {
-            int ob = 0;
-            if (lane == __ffs(m) - 1) ob = atomicAdd(&ncreated, __popc(m));
-            ob = __shfl_sync(kFull, ob, __ffs(m) - 1);
-            if (created) screated[ob + __popc(m & ((1u << lane) - 1))] = g + j;
-        }
-    }
-    // one reservation in the occupied list per chunk (the distinct count), then a
-    // coalesced copy: the chunks of one hub run together, so per-warp reservations
-    // would queue on the same counter
-    __syncthreads();
-    if (threadIdx.x == 0) obase = ncreated ? atomicAdd(dcount, ncreated) : 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < ncreated; i += kTB) occ[obase + i] = screated[i];
-    // the chunk's partial summary -> bpart (the key arrays are no longer read: reuse)
-    {
-        const int Ww = __reduce_max_sync(kFull, oW);
-        const bool top = oW == Ww;
-        const int kw = __reduce_add_sync(kFull, top ? ok : 0);
-        const int mnw = __reduce_min_sync(kFull, top ? omn : INT_MAX);
-        const int mxw = __reduce_max_sync(kFull, top ? omx : -1);
-        __syncthreads();
-        int *red = reinterpret_cast<int *>(skey);
-        if (lane == 0) {
-            red[warp] = Ww;
-            red[kNW + warp] = kw;
-            red[2 * kNW + warp] = mnw;
-            red[3 * kNW + warp] = mxw;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int Wb = 0, kb = 0, mnb = INT_MAX, mxb = -1;
-            for (int w = 0; w < kNW; ++w) Wb = max(Wb, red[w]);
-            for (int w = 0; w < kNW; ++w)
-                if (red[w] == Wb) {
-                    kb += red[kNW + w];
-                    mnb = min(mnb, red[2 * kNW + w]);
-                    mxb = max(mxb, red[3 * kNW + w]);
-                }
-            int *o = p.bpart + 4 * (int64_t)ch;
-            o[0] = Wb;
-            o[1] = kb;
-            o[2] = mnb;
-            o[3] = mxb;
+        // one reservation per partition among the warp's pairs
+        const unsigned grp = __match_any_sync(kFull, part);
+        const int leader = __ffs(grp) - 1;
+        int at = 0;
+        if (part >= 0 && lane == leader) at = atomicAdd(&p.pfill[q + part], __popc(grp));
+        at = __shfl_sync(kFull, at, leader) + __popc(grp & ((1u << lane) - 1));
+        if (part >= 0) {
+            if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)L << 32) | c;
+            else atomicOr(&p.ctl->err, kErrHubOverflow);
         }
     }
 }
 
 // Ranks of each big vertex's smallest and largest candidate among its distinct labels,
-// over the occupied slots of its table, one CTA per stats chunk; only vertices with
-// some but not all distinct labels tied at the maximum need them.
+// over its distinct list, one CTA per stats chunk; only vertices with some but not all
+// distinct labels tied at the maximum need them.
 __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p)
 {
     __shared__ int red[2][kNW];
@@ -1098,13 +996,12 @@ __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p)
     const int64_t i0 = p.schunk_s0[c];
     const int64_t i1 = min(p.schunk_s1[c], (int64_t)d);
     if (st.k == 1 || st.k == d || i0 >= i1) return;
-    const uint32_t *occ = p.big_occ + p.big_ooff[bi];
-    const unsigned long long *gt = p.gtab + p.big_toff[bi];
+    const unsigned long long *list = p.big_list + p.big_ooff[bi];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int cmn = st.cmin, cmx = st.cmax;
     int r0 = 0, r1 = 0;
     for (int64_t i = i0 + threadIdx.x; i < i1; i += kTB) {
-        const int lab = (int)((uint32_t)(gt[occ[i]] >> p.hub_cbits) & p.hub_lmask);
+        const int lab = (int)(list[i] >> 32);
         r0 += lab < cmn;
         r1 += lab < cmx;
     }
@@ -1126,8 +1023,8 @@ __global__ void __launch_bounds__(kTB) big_stats_kernel(IterArgs p)
     }
 }
 
-// One warp per big vertex: fold its insert chunks' partial summaries; when every
-// distinct label is a candidate the ranks are 0 and d - 1.
+// One warp per big vertex: fold its partitions' summaries; when every distinct label is
+// a candidate the ranks are 0 and d - 1.
 __global__ void big_combine_kernel(IterArgs p)
 {
     if (!ctl_active(p.ctl)) return;
@@ -1136,8 +1033,8 @@ __global__ void big_combine_kernel(IterArgs p)
     for (int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < p.nbig; i += nw) {
         const int bi = p.b0 + i;
         int W = 0, k = 0, mn = INT_MAX, mx = -1;
-        for (int c = p.big_c0[bi] + lane; c < p.big_c0[bi + 1]; c += 32) {
-            const int4 o = *reinterpret_cast<const int4 *>(p.bpart + 4 * (int64_t)c);
+        for (int c = p.hub_p0[bi] + lane; c < p.hub_p0[bi + 1]; c += 32) {
+            const int4 o = p.psum[c];
             if (o.x > W) {
                 W = o.x;
                 k = o.y;
@@ -1194,10 +1091,8 @@ __global__ void __launch_bounds__(32) big_resolve_kernel(IterArgs p)
         } else if (!sq.fail && r == st.rmax) {
             label = st.cmax;
         } else {
-            WarpTableQueryT<HubTable> q{{p.gtab + p.big_toff[bi], p.hub_cbits, p.hub_gshift, p.hub_lmask, p.hub_gen},
-                                        (int)p.big_tcap[bi], d, st.W, st.rmin, st.rmax, hist, lane, pick_scratch};
-            q.occ = p.big_occ + p.big_ooff[bi];
-            q.nocc = d;
+            WarpTableQueryT<DenseTable> q{{p.big_list + p.big_ooff[bi]}, d, d, st.W, st.rmin, st.rmax, hist, lane,
+                                          pick_scratch};
             if (sq.fail) r = resolve_rank(a, d, N, v == p.last_v, q);
             label = (r == st.rmin) ? st.cmin : (r == st.rmax) ? st.cmax : (int32_t)q.select(r);
         }

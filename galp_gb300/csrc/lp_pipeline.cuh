@@ -739,6 +739,74 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     flush_changes(changes, p.ctl);
 }
 
+// One CTA per hub partition (grid-stride over the scope's partitions): count the
+// partition's (label, count) pairs in a shared-memory table sized to them (all pairs of a
+// label fall in one partition, so its count is complete here), fold the counts each
+// insert observes into the partition's summary, append its distinct labels to the hub's
+// distinct list and reset the partition's fill for the next scope.
+__global__ void __launch_bounds__(kTB) hub_count_kernel(IterArgs p)
+{
+    extern __shared__ __align__(16) uint32_t hub_tab[];  // kHubTab keys, then kHubTab counts
+    __shared__ int red[5][32], red2[2][32];
+    __shared__ int sfill, sbase, sctr;
+    if (!ctl_active(p.ctl)) return;
+    uint32_t *key = hub_tab;
+    uint32_t *cnt = hub_tab + kHubTab;
+    const BlockRed5<kTB> br{red, red2};
+    const int tid = threadIdx.x, lane = tid & 31;
+    for (int x = blockIdx.x; x < p.nparts; x += gridDim.x) {
+        const int gp = p.q0 + x;
+        const int bi = p.part_big[gp];
+        const int pcap = p.hub_pcap[bi];
+        if (tid == 0) sfill = min(p.pfill[gp], pcap);
+        __syncthreads();
+        const int fill = sfill;
+        uint32_t tcap = 64;
+        while (tcap < 2u * (uint32_t)fill) tcap <<= 1;  // load <= 1/2; fill <= kHubPartCap
+        for (int s2 = tid; s2 < (int)tcap; s2 += kTB) {
+            key[s2] = kEmpty;
+            cnt[s2] = 0;
+        }
+        __syncthreads();
+        const unsigned long long *src = p.pairs + p.hub_pbase[bi] + (int64_t)(gp - p.hub_p0[bi]) * pcap;
+        Sum5 obs = sum5_empty();
+        for (int j = tid; j < fill; j += kTB) {
+            const unsigned long long xv = src[j];
+            const uint32_t L = (uint32_t)(xv >> 32), c = (uint32_t)xv;
+            uint32_t h = hslot(L, tcap);
+            for (;;) {
+                const uint32_t prev = atomicCAS(&key[h], kEmpty, L);
+                if (prev == kEmpty || prev == L) {
+                    obs.d += prev == kEmpty;
+                    sum5_observe(obs, (int)L, (int)(atomicAdd(&cnt[h], c) + c));
+                    break;
+                }
+                h = (h + 1 == tcap) ? 0 : h + 1;
+            }
+        }
+        const Sum5 sm = br.reduce(obs);  // its barrier also completes the table
+        if (tid == 0) {
+            sbase = sm.d ? atomicAdd(&p.bstat[bi].d, sm.d) : 0;
+            sctr = 0;
+            p.psum[gp] = make_int4(sm.W, sm.k, sm.mn, sm.mx);
+            p.pfill[gp] = 0;
+        }
+        __syncthreads();
+        unsigned long long *list = p.big_list + p.big_ooff[bi] + sbase;
+        for (int s0 = 0; s0 < (int)tcap; s0 += kTB) {
+            const int s2 = s0 + tid;
+            const bool used = s2 < (int)tcap && key[s2] != kEmpty;
+            const unsigned m = __ballot_sync(kFull, used);
+            if (!m) continue;
+            int at = 0;
+            if (lane == __ffs(m) - 1) at = atomicAdd(&sctr, __popc(m));
+            at = __shfl_sync(kFull, at, __ffs(m) - 1) + __popc(m & ((1u << lane) - 1));
+            if (used) list[at] = ((unsigned long long)key[s2] << 32) | cnt[s2];
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void big_dcnt_kernel(IterArgs a, int32_t *dcnt)
 {
     if (!ctl_active(a.ctl)) return;

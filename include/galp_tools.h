@@ -22,7 +22,7 @@ typedef struct {
     int64_t nmid;          /* vertices with 33..256 neighbours (one warp each) */
     int64_t nlarge;        /* vertices with 257..12288 neighbours (one CTA each, on-chip table) */
     int64_t nbig;          /* vertices on the global-table path */
-    int64_t table_slots;   /* global hash-table slots of those vertices (largest scope) */
+    int64_t table_slots;   /* pair slots of those vertices' hash partitions (largest scope) */
     int32_t launches_per_iter; /* kernels launched per dense iteration (upper bound) */
     int32_t flags;         /* GALP_SCHED_* bits */
     int64_t launches;      /* kernels launched by the context's runs so far (setup excluded) */
@@ -61,7 +61,10 @@ typedef struct {
     float learned_margin;  /* learned rule: predicted log gain needed to leave the fixed rule's
                               choice (default 0.03) */
     int32_t small_sort;    /* packs of small vertices: 1 = sort-based counting, 0 = match-based */
-    int32_t pad[4];
+    int32_t hub_part_shift; /* hubs (above 12288 neighbours) count their labels in degree * 2^shift / 2048
+                               hash partitions (default 0); a partition that overflows makes the run
+                               redo itself with the shift raised by one (up to 6) */
+    int32_t pad[3];
 } galp_variant;
 
 /* One row of the in-core variant table (every row computes the same labels). */

@@ -113,3 +113,25 @@ def test_hubs_inside_out_of_core_batches(hub_graph, policy, bpow):
             assert list(p.updates) == list(counts)
             if it < k:
                 break
+
+
+@pytest.mark.parametrize("shift", [-6, 2])
+def test_hub_partition_count_does_not_change_labels(hub_graph, shift):
+    """Hubs count their labels in hash partitions of degree * 2^shift / 2048 pairs each.
+    With far too few partitions (shift -6: one or two per hub, 4096 pairs each) the first
+    iterations overflow them; the run is redone with twice the partitions until none
+    overflows, and its labels are exact.  More partitions (shift 2) are exact too."""
+    with galp_gb300.Propagator(hub_graph) as p:
+        tools.set_variant(p, hub_part_shift=shift)
+        for k in (1, 2, 3, 10):
+            p.run(k)
+            it, want, counts = oracle.run(hub_graph.offsets, hub_graph.neighbors, k)
+            assert p.iters_run == it and list(p.updates) == list(counts)
+            assert np.array_equal(p.get_labels(), want)
+            if it < k:
+                break
+        v = tools.set_variant(p)
+        if shift < 0:
+            assert v.hub_part_shift > shift  # overflowed at least once and was redone
+        else:
+            assert v.hub_part_shift == shift
