@@ -116,9 +116,10 @@ constexpr int kMaxHubShift = 6;  // at most 64x the default hub partitions
 
 // Hash partitions of the big vertices: a hub of degree D gets ceil(D * 2^shift / 2048)
 // partitions (its chunks emit at most D pairs, about 2048 per partition while labels are
-// still mostly distinct), each holding 1.5x its share plus 256 pairs, at most
-// kHubPartCap.  Partition indices are global; pair areas are relative to the scope (out-of-
-// core batches reuse one area).
+// still mostly distinct).  A partition holds 1.5x its share plus 256 pairs, plus one pair
+// per insert chunk of the hub: a label that appears in every chunk (late iterations) sends
+// all its pairs to one partition.  Partition indices are global; pair areas are relative
+// to the scope (out-of-core batches reuse one area).
 void plan_hub_parts(Schedule &S, int shift)
 {
     const size_t nb = S.big_v.size();
@@ -135,7 +136,8 @@ void plan_hub_parts(Schedule &S, int shift)
             const int64_t deg = S.big_deg[(size_t)b];
             const double scaled = std::ldexp((double)deg, shift) / kHubPartPairs;
             const int64_t np = std::max<int64_t>(1, std::min<int64_t>((int64_t)std::ceil(scaled), deg));
-            const int64_t cap = std::min<int64_t>(kHubPartCap, (3 * deg + 2 * np - 1) / (2 * np) + 256);
+            const int64_t nchunks = (deg + kBigChunk - 1) / kBigChunk;
+            const int64_t cap = std::min<int64_t>(deg, (3 * deg + 2 * np - 1) / (2 * np) + 256 + nchunks);
             S.hub_p0[(size_t)b] = (int32_t)S.part_big.size();
             S.hub_pbase[(size_t)b] = pbase;
             S.hub_pcap[(size_t)b] = (int32_t)cap;

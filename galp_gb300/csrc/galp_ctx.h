@@ -89,8 +89,8 @@ struct Schedule {
 bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vector<int64_t> &scope_starts);
 
 // (Re)plan the hash partitions of every big vertex: degree * 2^shift / kHubPartPairs
-// partitions (at least one), each holding 1.5x its share of the degree plus 256 pairs,
-// at most kHubPartCap.
+// partitions (at least one), each holding 1.5x its share of the degree, plus 256 pairs,
+// plus one pair per insert chunk of the vertex (at most the degree).
 void plan_hub_parts(Schedule &S, int shift);
 
 // Batch boundaries of OutOfCore::compute_batch_boundaries (outofcore.cuh:38-60) for

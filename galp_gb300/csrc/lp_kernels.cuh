@@ -36,8 +36,7 @@ constexpr int kSmallMax = 32;         // degree handled by one warp pack
 constexpr int kBigChunk = 1024;       // edges per big_insert CTA
 constexpr int kBigSlotChunk = 8192;   // distinct-list entries per big_stats CTA
 constexpr int kHubPartPairs = 2048;   // target pairs per hub partition (a hub of degree D: D / 2048 partitions)
-constexpr int kHubPartCap = 4096;     // largest pair capacity of a partition (its table has 2x the slots)
-constexpr int kHubTab = 2 * kHubPartCap;
+constexpr int kHubTab = 8192;         // shared-memory table slots of a hub partition (distinct labels < 8192)
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
 constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound (about a second)
@@ -45,8 +44,8 @@ constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound 
 // error bits in Ctl::err
 constexpr int kErrLookback = 1;
 constexpr int kErrFormat = 2;
-constexpr int kErrHubOverflow = 4;  // a hub partition received more pairs than it holds (the run is redone
-                                    // with twice the partitions)
+constexpr int kErrHubOverflow = 4;  // a hub partition received more pairs, or more distinct labels, than it
+                                    // holds (the run is redone with twice the partitions)
 
 struct Ctl {
     int active;                 // 1 while iterations still run

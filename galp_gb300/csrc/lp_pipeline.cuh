@@ -761,8 +761,8 @@ __global__ void __launch_bounds__(kTB) hub_count_kernel(IterArgs p)
         if (tid == 0) sfill = min(p.pfill[gp], pcap);
         __syncthreads();
         const int fill = sfill;
-        uint32_t tcap = 64;
-        while (tcap < 2u * (uint32_t)fill) tcap <<= 1;  // load <= 1/2; fill <= kHubPartCap
+        uint32_t tcap = 64;  // load <= 1/2 when every pair is a distinct label
+        while (tcap < 2u * (uint32_t)fill && tcap < (uint32_t)kHubTab) tcap <<= 1;
         for (int s2 = tid; s2 < (int)tcap; s2 += kTB) {
             key[s2] = kEmpty;
             cnt[s2] = 0;
@@ -774,7 +774,13 @@ __global__ void __launch_bounds__(kTB) hub_count_kernel(IterArgs p)
             const unsigned long long xv = src[j];
             const uint32_t L = (uint32_t)(xv >> 32), c = (uint32_t)xv;
             uint32_t h = hslot(L, tcap);
-            for (;;) {
+            // a full table (more distinct labels than slots: pairs repeating few labels
+            // made it small) ends the probe after one round and flags the run
+            for (uint32_t probe = 0;; ++probe) {
+                if (probe == tcap) {
+                    atomicOr(&p.ctl->err, kErrHubOverflow);
+                    break;
+                }
                 const uint32_t prev = atomicCAS(&key[h], kEmpty, L);
                 if (prev == kEmpty || prev == L) {
                     obs.d += prev == kEmpty;
