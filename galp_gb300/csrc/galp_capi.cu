@@ -112,11 +112,11 @@ void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
 
 }  // namespace
 
-constexpr int kMaxHubShift = 6;  // at most 64x the default hub partitions
+constexpr int kMaxHubShift = 6;  // at most 64x the default hub partitions (and at most kHubMaxParts)
 
-// Hash partitions of the big vertices: a hub of degree D gets ceil(D * 2^shift / 2048)
-// partitions (its chunks emit at most D pairs, about 2048 per partition while labels are
-// still mostly distinct).  A partition holds 1.5x its share plus 256 pairs, plus one pair
+// Hash partitions of the big vertices: a hub of degree D gets ceil(D * 2^shift / 8192)
+// partitions, at most 2048 (its chunks emit at most D pairs, about 8192 per partition
+// while labels are still mostly distinct).  A partition holds 1.5x its share plus 256 pairs, plus one pair
 // per insert chunk of the hub: a label that appears in every chunk (late iterations) sends
 // all its pairs to one partition.  Partition indices are global; pair areas are relative
 // to the scope (out-of-core batches reuse one area).
@@ -135,7 +135,8 @@ void plan_hub_parts(Schedule &S, int shift)
         for (int32_t b = sc.b0; b < sc.b0 + sc.nb; ++b) {
             const int64_t deg = S.big_deg[(size_t)b];
             const double scaled = std::ldexp((double)deg, shift) / kHubPartPairs;
-            const int64_t np = std::max<int64_t>(1, std::min<int64_t>((int64_t)std::ceil(scaled), deg));
+            const int64_t np = std::max<int64_t>(
+                1, std::min<int64_t>(std::min<int64_t>((int64_t)std::ceil(scaled), deg), kHubMaxParts));
             const int64_t nchunks = (deg + kBigChunk - 1) / kBigChunk;
             const int64_t cap = std::min<int64_t>(deg, (3 * deg + 2 * np - 1) / (2 * np) + 256 + nchunks);
             S.hub_p0[(size_t)b] = (int32_t)S.part_big.size();
@@ -555,7 +556,7 @@ int Engine::setup_hub_parts(int shift, cudaStream_t st, int64_t &h2d)
         const int smem = (int)(sizeof(uint32_t) * 2 * kHubTab);
         GALP_CUDA(cudaFuncSetAttribute(hub_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         int occ = 0;
-        GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hub_count_kernel, kTB, smem));
+        GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hub_count_kernel, kHubCountThreads, smem));
         hub_count_blocks = std::max(occ, 1) * sms;
     }
     GALP_CUDA(cudaStreamSynchronize(st));
@@ -718,7 +719,8 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         if (prof.on) e0 = prof.mark(st);
         big_insert_kernel<<<a.nchunks, kTB, 0, st>>>(a);
         launched("big_insert_kernel", st);
-        hub_count_kernel<<<std::min(a.nparts, hub_count_blocks), kTB, sizeof(uint32_t) * 2 * kHubTab, st>>>(a);
+        hub_count_kernel<<<std::min(a.nparts, hub_count_blocks), kHubCountThreads, sizeof(uint32_t) * 2 * kHubTab,
+                           st>>>(a);
         launched("hub_count_kernel", st);
         big_combine_kernel<<<(a.nbig + 7) / 8, 256, 0, st>>>(a);
         launched("big_combine_kernel", st);

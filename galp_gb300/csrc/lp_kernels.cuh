@@ -35,8 +35,10 @@ constexpr int kTileV = 512;           // vertices per tile
 constexpr int kSmallMax = 32;         // degree handled by one warp pack
 constexpr int kBigChunk = 1024;       // edges per big_insert CTA
 constexpr int kBigSlotChunk = 8192;   // distinct-list entries per big_stats CTA
-constexpr int kHubPartPairs = 2048;   // target pairs per hub partition (a hub of degree D: D / 2048 partitions)
-constexpr int kHubTab = 8192;         // shared-memory table slots of a hub partition (distinct labels < 8192)
+constexpr int kHubPartPairs = 8192;   // target pairs per hub partition (a hub of degree D: D / 8192 partitions)
+constexpr int kHubTab = 16384;        // shared-memory table slots of a hub partition (distinct labels < 16384)
+constexpr int kHubMaxParts = 2048;    // partitions of one hub at most (a chunk bins its pairs in shared memory)
+constexpr int kHubCountThreads = 1024;
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
 constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound (about a second)
@@ -892,11 +894,14 @@ __device__ __forceinline__ uint32_t hub_part(uint32_t label, uint32_t nparts)
 // reservation per warp and partition; appends to a partition are contiguous, so its
 // sectors fill in L2).  A partition that is full drops the pair and flags the run, which
 // the host then redoes with twice the partitions.
-__global__ void __launch_bounds__(kTB, 8) big_insert_kernel(IterArgs p)
+__global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
 {
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
     __shared__ uint16_t sused[kBigChunk];     // occupied local slots, compacted
+    __shared__ uint16_t spart[kBigChunk];     // partition of each compacted pair
+    __shared__ uint16_t srank[kBigChunk];     // its position among the chunk's pairs of that partition
+    __shared__ int sbin[kHubMaxParts];        // pairs per partition, then the partition's reserved base
     __shared__ int nused;
     if (!ctl_active(p.ctl)) return;
     if ((int)blockIdx.x >= p.nchunks) return;
@@ -954,29 +959,30 @@ __global__ void __launch_bounds__(kTB, 8) big_insert_kernel(IterArgs p)
     __syncthreads();
     const int nloc = nused;
     const int q = p.hub_p0[bi];
-    const uint32_t np = (uint32_t)(p.hub_p0[bi + 1] - q);
+    const int np = p.hub_p0[bi + 1] - q;  // <= kHubMaxParts
     const int pcap = p.hub_pcap[bi];
     unsigned long long *area = p.pairs + p.hub_pbase[bi];
-    for (int base = 0; base < nloc; base += kTB) {  // block-uniform trip count
-        const int i = base + threadIdx.x;
-        uint32_t L = kEmpty, c = 0;
-        int part = -1;
-        if (i < nloc) {
-            const uint32_t ls = sused[i];
-            L = skey[ls];
-            c = scnt[ls];
-            part = (int)hub_part(L, np);
-        }
-        // one reservation per partition among the warp's pairs
-        const unsigned grp = __match_any_sync(kFull, part);
-        const int leader = __ffs(grp) - 1;
-        int at = 0;
-        if (part >= 0 && lane == leader) at = atomicAdd(&p.pfill[q + part], __popc(grp));
-        at = __shfl_sync(kFull, at, leader) + __popc(grp & ((1u << lane) - 1));
-        if (part >= 0) {
-            if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)L << 32) | c;
-            else atomicOr(&p.ctl->err, kErrHubOverflow);
-        }
+    // bin the chunk's pairs by partition, then one reservation per partition touched:
+    // the chunk's pairs of a partition land side by side
+    for (int b = threadIdx.x; b < np; b += kTB) sbin[b] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < nloc; i += kTB) {
+        const int part = (int)hub_part(skey[sused[i]], (uint32_t)np);
+        spart[i] = (uint16_t)part;
+        srank[i] = (uint16_t)atomicAdd(&sbin[part], 1);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < np; b += kTB) {
+        const int cnt = sbin[b];
+        if (cnt) sbin[b] = atomicAdd(&p.pfill[q + b], cnt);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nloc; i += kTB) {
+        const int part = spart[i];
+        const int at = sbin[part] + srank[i];
+        const uint32_t ls = sused[i];
+        if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)skey[ls] << 32) | scnt[ls];
+        else atomicOr(&p.ctl->err, kErrHubOverflow);
     }
 }
 

@@ -744,15 +744,16 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
 // label fall in one partition, so its count is complete here), fold the counts each
 // insert observes into the partition's summary, append its distinct labels to the hub's
 // distinct list and reset the partition's fill for the next scope.
-__global__ void __launch_bounds__(kTB) hub_count_kernel(IterArgs p)
+__global__ void __launch_bounds__(kHubCountThreads, 1) hub_count_kernel(IterArgs p)
 {
+    constexpr int kT = kHubCountThreads;
     extern __shared__ __align__(16) uint32_t hub_tab[];  // kHubTab keys, then kHubTab counts
     __shared__ int red[5][32], red2[2][32];
     __shared__ int sfill, sbase, sctr;
     if (!ctl_active(p.ctl)) return;
     uint32_t *key = hub_tab;
     uint32_t *cnt = hub_tab + kHubTab;
-    const BlockRed5<kTB> br{red, red2};
+    const BlockRed5<kT> br{red, red2};
     const int tid = threadIdx.x, lane = tid & 31;
     for (int x = blockIdx.x; x < p.nparts; x += gridDim.x) {
         const int gp = p.q0 + x;
@@ -763,14 +764,14 @@ __global__ void __launch_bounds__(kTB) hub_count_kernel(IterArgs p)
         const int fill = sfill;
         uint32_t tcap = 64;  // load <= 1/2 when every pair is a distinct label
         while (tcap < 2u * (uint32_t)fill && tcap < (uint32_t)kHubTab) tcap <<= 1;
-        for (int s2 = tid; s2 < (int)tcap; s2 += kTB) {
+        for (int s2 = tid; s2 < (int)tcap; s2 += kT) {
             key[s2] = kEmpty;
             cnt[s2] = 0;
         }
         __syncthreads();
         const unsigned long long *src = p.pairs + p.hub_pbase[bi] + (int64_t)(gp - p.hub_p0[bi]) * pcap;
         Sum5 obs = sum5_empty();
-        for (int j = tid; j < fill; j += kTB) {
+        for (int j = tid; j < fill; j += kT) {
             const unsigned long long xv = src[j];
             const uint32_t L = (uint32_t)(xv >> 32), c = (uint32_t)xv;
             uint32_t h = hslot(L, tcap);
@@ -799,7 +800,7 @@ __global__ void __launch_bounds__(kTB) hub_count_kernel(IterArgs p)
         }
         __syncthreads();
         unsigned long long *list = p.big_list + p.big_ooff[bi] + sbase;
-        for (int s0 = 0; s0 < (int)tcap; s0 += kTB) {
+        for (int s0 = 0; s0 < (int)tcap; s0 += kT) {
             const int s2 = s0 + tid;
             const bool used = s2 < (int)tcap && key[s2] != kEmpty;
             const unsigned m = __ballot_sync(kFull, used);

@@ -61,7 +61,7 @@ typedef struct {
     float learned_margin;  /* learned rule: predicted log gain needed to leave the fixed rule's
                               choice (default 0.03) */
     int32_t small_sort;    /* packs of small vertices: 1 = sort-based counting, 0 = match-based */
-    int32_t hub_part_shift; /* hubs (above 12288 neighbours) count their labels in degree * 2^shift / 2048
+    int32_t hub_part_shift; /* hubs (above 12288 neighbours) count their labels in degree * 2^shift / 8192
                                hash partitions (default 0); a partition that overflows makes the run
                                redo itself with the shift raised by one (up to 6) */
     int32_t pad[3];

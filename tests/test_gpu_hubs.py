@@ -117,10 +117,11 @@ def test_hubs_inside_out_of_core_batches(hub_graph, policy, bpow):
 
 @pytest.mark.parametrize("shift", [-6, 2])
 def test_hub_partition_count_does_not_change_labels(hub_graph, shift):
-    """Hubs count their labels in hash partitions of degree * 2^shift / 2048 pairs each.
-    With far too few partitions (shift -6: one or two per hub, 4096 pairs each) the first
-    iterations overflow them; the run is redone with twice the partitions until none
-    overflows, and its labels are exact.  More partitions (shift 2) are exact too."""
+    """Hubs count their labels in degree * 2^shift / 8192 hash partitions (at most 2048).
+    With far too few partitions (shift -6: one per hub, whose table holds fewer distinct
+    labels than the hub's neighbours carry) the first iterations overflow them; the run is
+    redone with twice the partitions until none overflows, and its labels are exact.  More
+    partitions (shift 2) are exact too."""
     with galp_gb300.Propagator(hub_graph) as p:
         tools.set_variant(p, hub_part_shift=shift)
         for k in (1, 2, 3, 10):
