@@ -599,6 +599,16 @@ def run_gpu(args, g, desc, rank, world, dist):
                 "alg_bytes": int(8 * m + 16 * n + 8), "dense_iteration_ms": round(it_dense, 4),
                 "achieved": round(whole, 1), "frac": round(whole / peak, 4),
                 "first_iteration_ms": round(kt.first_ms / max(kt.first_groups, 1), 4) if kt.first_groups else None}
+    if not args.policy:
+        # the gather floor: one pass that only streams the neighbour IDs and gathers their
+        # labels (random 4-byte loads, one L2 sector each) -- what any exact update pays
+        g_ms = tools.probe_gather(p, 5)
+        if g_ms > 0 and "whole_iteration" in roofline:
+            it_d = roofline["whole_iteration"]["dense_iteration_ms"]
+            roofline["gather_floor"] = {
+                "ms_per_pass": round(g_ms, 4), "G_gathers_per_s": round(m / (g_ms / 1e3) / 1e9, 1),
+                "hbm_GBps": round(8 * m / (g_ms / 1e3) / 1e9, 1),
+                "dense_iteration_vs_floor": round(g_ms / it_d, 4)}
     if args.policy:  # out-of-core: the neighbours cross the host link every iteration
         roofline["h2d_GBps_per_iteration"] = round(4 * m / (ms_per_step / NITER / 1e3) / 1e9, 1)
     p.close()

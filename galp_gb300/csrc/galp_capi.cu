@@ -1220,6 +1220,41 @@ void galp_destroy(galp_ctx *ctx)
     delete ctx;
 }
 
+int galp_probe_gather(galp_ctx *ctx, int32_t reps, float *ms_per_pass)
+{
+    if (!ctx || reps < 1 || !ms_per_pass) return GALP_EINVAL;
+    const galp::Engine &E = ctx->eng;
+    if (E.policy != 0 || E.batched) return GALP_EUNSUPPORTED;
+    GALP_CUDA(cudaSetDevice(ctx->opts.device));
+    unsigned long long *acc = (unsigned long long *)E.b_chk.p;  // 5 words from setup's checks
+    if (!acc || ctx->m == 0) {
+        *ms_per_pass = 0.f;
+        return GALP_OK;
+    }
+    const int blocks = E.sms * 8;
+    galp::gather_probe_kernel<<<blocks, galp::kTB, 0, ctx->stream>>>((const int32_t *)E.b_nbr[0].p, ctx->m,
+                                                                      (const int32_t *)E.b_lab0.p, acc);
+    GALP_CUDA(cudaGetLastError());
+    cudaEvent_t e0, e1;
+    GALP_CUDA(cudaEventCreate(&e0));
+    GALP_CUDA(cudaEventCreate(&e1));
+    cudaEventRecord(e0, ctx->stream);
+    for (int r = 0; r < reps; ++r)
+        galp::gather_probe_kernel<<<blocks, galp::kTB, 0, ctx->stream>>>((const int32_t *)E.b_nbr[0].p, ctx->m,
+                                                                          (const int32_t *)E.b_lab0.p, acc);
+    cudaEventRecord(e1, ctx->stream);
+    const cudaError_t le = cudaGetLastError();
+    const cudaError_t se = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    GALP_CUDA(le);
+    GALP_CUDA(se);
+    *ms_per_pass = ms / (float)reps;
+    return GALP_OK;
+}
+
 int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
 {
     if (!ctx || !info) return GALP_EINVAL;

@@ -814,6 +814,30 @@ __global__ void __launch_bounds__(kHubCountThreads, 1) hub_count_kernel(IterArgs
     }
 }
 
+// Measurement probe: one pass over the CSR that streams every neighbour ID and gathers its
+// label with the loads the counting kernels use (streaming IDs, evict-last label gathers),
+// 8 entries per thread in flight, and nothing else; the block XORs the labels into one
+// word.  Its time is the floor of any update that gathers every neighbour's label.
+__global__ void __launch_bounds__(kTB) gather_probe_kernel(const int32_t *nbr, int64_t m, const int32_t *lab,
+                                                           unsigned long long *acc)
+{
+    constexpr int PER = 8;
+    uint32_t x = 0;
+    const int64_t stride = (int64_t)gridDim.x * kTB * PER;
+    for (int64_t base = (int64_t)blockIdx.x * kTB * PER + threadIdx.x; base < m; base += stride) {
+        int nb[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int64_t e = base + (int64_t)u * kTB;
+            nb[u] = e < m ? ld_nbr(&nbr[e]) : -1;
+        }
+#pragma unroll
+        for (int u = 0; u < PER; ++u) x ^= nb[u] >= 0 ? (uint32_t)ld_label(&lab[nb[u]]) : 0u;
+    }
+    x = __reduce_xor_sync(kFull, x);
+    if ((threadIdx.x & 31) == 0 && x) atomicXor(acc, (unsigned long long)x);
+}
+
 __global__ void big_dcnt_kernel(IterArgs a, int32_t *dcnt)
 {
     if (!ctl_active(a.ctl)) return;

@@ -54,6 +54,19 @@ def _lib():
     return L
 
 
+def probe_gather(prop, reps: int = 5) -> float:
+    """Mean ms of one pass that streams every neighbour ID and gathers its label (the
+    gather floor of an iteration; include/galp_tools.h galp_probe_gather)."""
+    L = _lib()
+    L.galp_probe_gather.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_float)]
+    L.galp_probe_gather.restype = ctypes.c_int
+    ms = ctypes.c_float()
+    rc = L.galp_probe_gather(prop._h, reps, ctypes.byref(ms))
+    if rc:
+        raise RuntimeError(f"galp_probe_gather: {rc}")
+    return float(ms.value)
+
+
 def schedule_info(prop) -> SchedInfo:
     s = SchedInfo()
     rc = _lib().galp_schedule_info(prop._h, ctypes.byref(s))

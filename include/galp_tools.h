@@ -87,6 +87,10 @@ typedef struct {
 } galp_tune_result;
 
 int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info);
+/* Gather floor of an in-core context: mean device time (ms, CUDA events on the context's
+ * stream) of `reps` passes that stream every neighbour ID of the resident CSR and gather
+ * its label, with the loads of the counting kernels and no other work. */
+int galp_probe_gather(galp_ctx *ctx, int32_t reps, float *ms_per_pass);
 /* Launch-shape autotuner of a batched context (galp_batch_create): times probe runs of
  * niter iterations and keeps the fastest blocks-per-SM of the counting/resolve kernels. */
 int galp_batch_tune(galp_ctx *ctx, int32_t niter, galp_tune_result *res);
