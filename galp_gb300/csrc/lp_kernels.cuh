@@ -39,6 +39,7 @@ constexpr int kHubPartPairs = 8192;   // target pairs per hub partition (a hub o
 constexpr int kHubTab = 16384;        // shared-memory table slots of a hub partition (distinct labels < 16384)
 constexpr int kHubMaxParts = 2048;    // partitions of one hub at most (a chunk bins its pairs in shared memory)
 constexpr int kHubCountThreads = 1024;
+constexpr int kHubBinMin = 256;       // a chunk with this many pairs bins them by partition in shared memory
 constexpr unsigned kFull = 0xFFFFFFFFu;
 constexpr int kPickScratch = 8192;    // power of two >= kTile, for WarpTableQuery::tile_pick
 constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound (about a second)
@@ -962,27 +963,51 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
     const int np = p.hub_p0[bi + 1] - q;  // <= kHubMaxParts
     const int pcap = p.hub_pcap[bi];
     unsigned long long *area = p.pairs + p.hub_pbase[bi];
-    // bin the chunk's pairs by partition, then one reservation per partition touched:
-    // the chunk's pairs of a partition land side by side
-    for (int b = threadIdx.x; b < np; b += kTB) sbin[b] = 0;
-    __syncthreads();
-    for (int i = threadIdx.x; i < nloc; i += kTB) {
-        const int part = (int)hub_part(skey[sused[i]], (uint32_t)np);
-        spart[i] = (uint16_t)part;
-        srank[i] = (uint16_t)atomicAdd(&sbin[part], 1);
+    if (nloc >= kHubBinMin) {
+        // many pairs (labels still mostly distinct): bin them by partition, then one
+        // reservation per partition touched; the chunk's pairs of a partition land side by side
+        for (int b = threadIdx.x; b < np; b += kTB) sbin[b] = 0;
+        __syncthreads();
+        for (int i = threadIdx.x; i < nloc; i += kTB) {
+            const int part = (int)hub_part(skey[sused[i]], (uint32_t)np);
+            spart[i] = (uint16_t)part;
+            srank[i] = (uint16_t)atomicAdd(&sbin[part], 1);
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < np; b += kTB) {
+            const int cnt = sbin[b];
+            if (cnt) sbin[b] = atomicAdd(&p.pfill[q + b], cnt);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < nloc; i += kTB) {
+            const int part = spart[i];
+            const int at = sbin[part] + srank[i];
+            const uint32_t ls = sused[i];
+            if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)skey[ls] << 32) | scnt[ls];
+            else atomicOr(&p.ctl->err, kErrHubOverflow);
+        }
+        return;
     }
-    __syncthreads();
-    for (int b = threadIdx.x; b < np; b += kTB) {
-        const int cnt = sbin[b];
-        if (cnt) sbin[b] = atomicAdd(&p.pfill[q + b], cnt);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nloc; i += kTB) {
-        const int part = spart[i];
-        const int at = sbin[part] + srank[i];
-        const uint32_t ls = sused[i];
-        if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)skey[ls] << 32) | scnt[ls];
-        else atomicOr(&p.ctl->err, kErrHubOverflow);
+    // few pairs (labels repeat): one reservation per partition among a warp's pairs
+    for (int base = 0; base < nloc; base += kTB) {  // block-uniform trip count
+        const int i = base + threadIdx.x;
+        uint32_t L = kEmpty, c = 0;
+        int part = -1;
+        if (i < nloc) {
+            const uint32_t ls = sused[i];
+            L = skey[ls];
+            c = scnt[ls];
+            part = (int)hub_part(L, (uint32_t)np);
+        }
+        const unsigned grp = __match_any_sync(kFull, part);
+        const int leader = __ffs(grp) - 1;
+        int at = 0;
+        if (part >= 0 && lane == leader) at = atomicAdd(&p.pfill[q + part], __popc(grp));
+        at = __shfl_sync(kFull, at, leader) + __popc(grp & ((1u << lane) - 1));
+        if (part >= 0) {
+            if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)L << 32) | c;
+            else atomicOr(&p.ctl->err, kErrHubOverflow);
+        }
     }
 }
 

@@ -771,24 +771,34 @@ __global__ void __launch_bounds__(kHubCountThreads, 1) hub_count_kernel(IterArgs
         __syncthreads();
         const unsigned long long *src = p.pairs + p.hub_pbase[bi] + (int64_t)(gp - p.hub_p0[bi]) * pcap;
         Sum5 obs = sum5_empty();
-        for (int j = tid; j < fill; j += kT) {
-            const unsigned long long xv = src[j];
-            const uint32_t L = (uint32_t)(xv >> 32), c = (uint32_t)xv;
-            uint32_t h = hslot(L, tcap);
-            // a full table (more distinct labels than slots: pairs repeating few labels
-            // made it small) ends the probe after one round and flags the run
-            for (uint32_t probe = 0;; ++probe) {
-                if (probe == tcap) {
-                    atomicOr(&p.ctl->err, kErrHubOverflow);
-                    break;
+        constexpr int PER = 8;  // a thread's pair loads in flight together
+        for (int j0 = 0; j0 < fill; j0 += kT * PER) {
+            unsigned long long xs[PER];
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                const int j = j0 + tid + u * kT;
+                xs[u] = j < fill ? src[j] : ~0ull;  // a pair is never all ones (labels < 2^31)
+            }
+#pragma unroll
+            for (int u = 0; u < PER; ++u) {
+                if (xs[u] == ~0ull) continue;
+                const uint32_t L = (uint32_t)(xs[u] >> 32), c = (uint32_t)xs[u];
+                uint32_t h = hslot(L, tcap);
+                // a full table (more distinct labels than slots: pairs repeating few labels
+                // made it small) ends the probe after one round and flags the run
+                for (uint32_t probe = 0;; ++probe) {
+                    if (probe == tcap) {
+                        atomicOr(&p.ctl->err, kErrHubOverflow);
+                        break;
+                    }
+                    const uint32_t prev = atomicCAS(&key[h], kEmpty, L);
+                    if (prev == kEmpty || prev == L) {
+                        obs.d += prev == kEmpty;
+                        sum5_observe(obs, (int)L, (int)(atomicAdd(&cnt[h], c) + c));
+                        break;
+                    }
+                    h = (h + 1 == tcap) ? 0 : h + 1;
                 }
-                const uint32_t prev = atomicCAS(&key[h], kEmpty, L);
-                if (prev == kEmpty || prev == L) {
-                    obs.d += prev == kEmpty;
-                    sum5_observe(obs, (int)L, (int)(atomicAdd(&cnt[h], c) + c));
-                    break;
-                }
-                h = (h + 1 == tcap) ? 0 : h + 1;
             }
         }
         const Sum5 sm = br.reduce(obs);  // its barrier also completes the table
