@@ -348,7 +348,8 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     max_label = n;
     if (policy != 0 && (o.buffer_pow < 1 || o.buffer_pow > 40)) return GALP_EINVAL;
     GALP_CUDA(b_off.alloc(sizeof(int64_t) * (n + 1)));
-    if (policy == 0) GALP_CUDA(b_nbr[0].alloc(sizeof(int32_t) * std::max<int64_t>(m, 1)));
+    // 16 bytes of padding: bulk copies of a vertex's neighbours end at a 16-byte boundary
+    if (policy == 0) GALP_CUDA(b_nbr[0].alloc(sizeof(int32_t) * std::max<int64_t>(m, 1) + 16));
     // the CSR upload runs while the host builds the schedule (host or device neighbours:
     // batched callers may hand over a device array)
     GALP_CUDA(cudaMemcpyAsync(b_off.p, g.offsets, sizeof(int64_t) * (n + 1), cudaMemcpyDefault, st));
@@ -369,7 +370,7 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     phase(0);
 
     if (policy != 0) {
-        const size_t cap = sizeof(int32_t) * std::max<int64_t>(sched.max_scope_edges, 1);
+        const size_t cap = sizeof(int32_t) * std::max<int64_t>(sched.max_scope_edges, 1) + 16;
         GALP_CUDA(b_nbr[0].alloc(cap));
         GALP_CUDA(b_nbr[1].alloc(cap));
         // pin the caller's neighbours for asynchronous copies (graph.h:108-111 pins them too)
@@ -743,14 +744,23 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
                                                     (int64_t)sms * std::min(mid_bps, occ_mid)),
                              32 * kMidWarps, 0, st>>>(q);
         launched("count_mid64_kernel", st);
-        count_cta_kernel<128, 2 * kLargeAMax>
-            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 10)), 128,
-               sizeof(unsigned long long) * 2 * kLargeAMax, st>>>(q, 0);
-        launched("count_cta_kernel<128>", st);
-        count_cta_kernel<kTB, 2 * kLargeMax>
-            <<<(int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * 5)), kTB,
-               sizeof(unsigned long long) * 2 * kLargeMax, st>>>(q, 1);
-        launched("count_cta_kernel<256>", st);
+        const int g128 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 10));
+        const int g256 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * 5));
+        if (variant.cta_stage) {  // neighbour IDs staged by bulk copies (the stage follows the table)
+            count_cta_kernel<128, 2 * kLargeAMax, true>
+                <<<g128, 128, sizeof(unsigned long long) * 2 * kLargeAMax + sizeof(int32_t) * (kLargeAMax + 8), st>>>(
+                    q, 0);
+            launched("count_cta_kernel<128>", st);
+            count_cta_kernel<kTB, 2 * kLargeMax, true>
+                <<<g256, kTB, sizeof(unsigned long long) * 2 * kLargeMax + sizeof(int32_t) * (kLargeMax + 8), st>>>(
+                    q, 1);
+            launched("count_cta_kernel<256>", st);
+        } else {
+            count_cta_kernel<128, 2 * kLargeAMax><<<g128, 128, sizeof(unsigned long long) * 2 * kLargeAMax, st>>>(q, 0);
+            launched("count_cta_kernel<128>", st);
+            count_cta_kernel<kTB, 2 * kLargeMax><<<g256, kTB, sizeof(unsigned long long) * 2 * kLargeMax, st>>>(q, 1);
+            launched("count_cta_kernel<256>", st);
+        }
         if (q.nmid_x + q.nmid_l) {
             count_cta_kernel<512, 2 * kXlAMax>
                 <<<(int)std::max<int64_t>(1, std::min<int64_t>(q.nmid_x + q.nmid_l, (int64_t)sms * 2)), 512,
@@ -1166,7 +1176,7 @@ int galp_sync(galp_ctx *ctx, galp_stats *st)
     }
     if (c.err & kErrFormat) return GALP_EFORMAT;
     if (c.err & kErrHubOverflow) return GALP_ENOMEM;
-    return (c.err & kErrLookback) ? GALP_ETIMEOUT : GALP_OK;
+    return (c.err & (kErrLookback | kErrStage)) ? GALP_ETIMEOUT : GALP_OK;
 }
 
 int galp_run(galp_ctx *ctx, int32_t niter, galp_stats *st)
@@ -1284,7 +1294,8 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
 int galp_set_variant(galp_ctx *ctx, const galp_variant *v)
 {
     if (!ctx || !v || v->agg_mode < 0 || v->agg_mode > 2 || !(v->frontier_frac >= 0.f && v->frontier_frac <= 1.f) ||
-        !(v->learned_margin >= 0.f && v->learned_margin < 10.f) || v->small_sort < 0 || v->small_sort > 1)
+        !(v->learned_margin >= 0.f && v->learned_margin < 10.f) || v->small_sort < 0 || v->small_sort > 1 ||
+        v->cta_stage < 0 || v->cta_stage > 1)
         return GALP_EINVAL;
     if (v->hub_part_shift < -16 || v->hub_part_shift > kMaxHubShift) return GALP_EINVAL;
     if (v->hub_part_shift != ctx->eng.sched.hub_shift) {

@@ -47,6 +47,7 @@ constexpr long long kSpinLimit = 1ll << 20;  // default look-back give-up bound 
 // error bits in Ctl::err
 constexpr int kErrLookback = 1;
 constexpr int kErrFormat = 2;
+constexpr int kErrStage = 8;        // a bulk-copy wait of a counting kernel ran out (bounded wait)
 constexpr int kErrHubOverflow = 4;  // a hub partition received more pairs, or more distinct labels, than it
                                     // holds (the run is redone with twice the partitions)
 

@@ -659,15 +659,69 @@ struct BlockRed5 {
     }
 };
 
+// ----- bulk copies into shared memory (cp.async.bulk) with mbarrier completion -----
+__device__ __forceinline__ uint32_t smem_u32(const void *ptr)
+{
+    return (uint32_t)__cvta_generic_to_shared(ptr);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// One thread: expect `bytes` on the barrier, then copy them global -> shared (both
+// addresses 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the barrier's phase `parity`; false after kStageSpinLimit polls.
+constexpr long long kStageSpinLimit = 1ll << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity)
+{
+    for (long long i = 0; i < kStageSpinLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
 // One CTA of THREADS threads per vertex of degree <= SLOTS/2 (table of SLOTS 64-bit
 // slots in dynamic shared memory), for a range of the degree-sorted mid list.
-template <int THREADS, int SLOTS>
+//
+// STAGE: the next vertex's neighbour IDs are copied into a shared-memory stage by one
+// bulk copy (cp.async.bulk, completion on an mbarrier) while the current vertex is
+// counted, so the IDs are read from shared memory and no thread waits on their global
+// loads.  The copy starts at the 16-byte boundary below the vertex's first entry and
+// ends at the one above its last (the neighbour buffers carry 16 bytes of padding).  A
+// wait that runs out (it cannot for a valid address) sets kErrStage, waits for that copy
+// once more before the CTA exits and counts the remaining vertices from global loads.
+// Not in frontier mode (clean vertices need no IDs).
+template <int THREADS, int SLOTS, bool STAGE = false>
 __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 ? 2 : THREADS >= 256 ? 5 : 10)
     count_cta_kernel(PipeArgs p, int which)
 {
     extern __shared__ __align__(16) unsigned long long cta_tab[];
     __shared__ int red[5][32], red2[2][32];
     __shared__ int sctr;
+    __shared__ __align__(8) unsigned long long stage_bar;
+    __shared__ int stage_ok;
     if (!ctl_active(p.ctl)) return;
     // ranges of the degree-sorted mid list: 0 [pos1, pos_a), 1 [pos_a, pos2), 2 [pos2, pos_b),
     // 3 [pos_b, end)
@@ -681,6 +735,26 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     unsigned long long changes = 0;
     for (int s = tid; s < SLOTS; s += THREADS) cta_tab[s] = 0ull;
     uint32_t gen = 0;
+    // staging: thread 0 copies the neighbour IDs of list entry i into the stage
+    const bool staged = STAGE && !fr;
+    int32_t *stage = reinterpret_cast<int32_t *>(cta_tab + SLOTS);
+    uint32_t parity = 0, lost_parity = 2;
+    auto stage_issue = [&](int i) {
+        if (i >= count) return;
+        const int vn = p.mid_v[first + i];
+        const int64_t a = __ldg(&p.off[vn]) - p.nbr_shift;
+        const int64_t b = __ldg(&p.off[vn + 1]) - p.nbr_shift;
+        const int64_t a4 = a & ~(int64_t)3, b4 = (b + 3) & ~(int64_t)3;
+        // the proxy fence orders the threads' reads of the stage before the copy's writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        bulk_load(stage, p.nbr + a4, (uint32_t)(4 * (b4 - a4)), &stage_bar);
+    };
+    if (staged && tid == 0) {
+        mbar_init(&stage_bar, 1);
+        stage_ok = 1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stage_issue(blockIdx.x);
+    }
     __syncthreads();
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         const int v = p.mid_v[first + i];
@@ -695,6 +769,20 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
         }
         const int64_t o0 = __ldg(&p.off[v]);
         const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
+        // this vertex's IDs in the stage (the copy was issued one vertex earlier)
+        bool from_stage = false;
+        if (staged && stage_ok) {
+            const bool got = mbar_wait(&stage_bar, parity);
+            if (!got) stage_ok = 0;  // any thread that gave up turns staging off for the CTA
+            __syncthreads();
+            from_stage = stage_ok != 0;
+            if (!from_stage) {
+                lost_parity = parity;  // the copy still in flight completes this phase
+                if (tid == 0) atomicOr(&p.ctl->err, kErrStage);
+            }
+            parity ^= 1u;
+        }
+        const int skip = (int)((o0 - p.nbr_shift) & 3);
         // probe range: the whole table up to 4 slots per neighbour (load <= 1/4 where the
         // table allows, at most 1/2): the longest probe of a warp's inserts sets its pace
         const uint32_t cap = (uint32_t)min(SLOTS, 4 * pad32(deg));
@@ -707,7 +795,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
 #pragma unroll
             for (int u = 0; u < PER; ++u) {
                 const int e = base + tid + u * THREADS;
-                nb[u] = (e < deg) ? ld_nbr(&p.nbr[o0 + e - p.nbr_shift]) : -1;
+                nb[u] = (e < deg) ? (from_stage ? stage[skip + e] : ld_nbr(&p.nbr[o0 + e - p.nbr_shift])) : -1;
             }
             uint32_t lb[PER];
 #pragma unroll
@@ -718,8 +806,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
                 t64_insert_row(cta_tab, cap, gen, lb[u], agg, obs);
             }
         }
-        // the reduction's barrier also completes the table for the rank and spill passes
+        // the reduction's barrier also completes the table for the rank and spill passes,
+        // and every thread's reads of the stage: the next vertex's copy may start
         const Sum5 s = br.reduce(obs);
+        if (from_stage && tid == 0) stage_issue(i + gridDim.x);
         int rmin = 0, rmax = s.d - 1;  // when every distinct label is a candidate
         if (s.k > 1) {
             if (s.k < s.d) {
@@ -736,6 +826,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
         if (tid == 0) finish_counted(p, v, s, rmin, rmax, changes);
         __syncthreads();
     }
+    // a copy that a wait gave up on still lands in this CTA's shared memory: wait for it
+    // (bounded) before the CTA exits
+    if (staged && lost_parity < 2) (void)mbar_wait(&stage_bar, lost_parity);
     flush_changes(changes, p.ctl);
 }
 

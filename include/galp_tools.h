@@ -64,7 +64,9 @@ typedef struct {
     int32_t hub_part_shift; /* hubs (above 12288 neighbours) count their labels in degree * 2^shift / 8192
                                hash partitions (default 0); a partition that overflows makes the run
                                redo itself with the shift raised by one (up to 6) */
-    int32_t pad[3];
+    int32_t cta_stage;      /* CTA counting of 257..2048 neighbours: 1 = the next vertex's neighbour IDs
+                               staged in shared memory by a bulk copy (default), 0 = global loads */
+    int32_t pad[2];
 } galp_variant;
 
 /* One row of the in-core variant table (every row computes the same labels). */

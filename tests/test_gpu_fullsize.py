@@ -70,3 +70,22 @@ def test_lfr_1m_ten_iterations_equal_the_oracle():
         it, want, counts = oracle.run(g.offsets, g.neighbors, 10)
         assert its == it and upd == list(counts)
         assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("stage", [0, 1])
+def test_cta_staging_on_and_off_equal_the_oracle(stage):
+    # CTA counting with the next vertex's neighbour IDs staged by bulk copies (default) or
+    # read from global memory: the same labels, in-core and out of core
+    from galp_gb300 import tools
+
+    g = galp_gb300.generate_rmat(17, 24, seed=11)
+    assert ((g.degrees() > 256) & (g.degrees() <= 2048)).sum() > 100
+    for opts in ({}, {"policy": 2, "buffer_pow": 18}):
+        with galp_gb300.Propagator(g, early_exit=0, **opts) as p:
+            tools.set_variant(p, cta_stage=stage)
+            want = np.arange(g.n, dtype=np.int32)
+            for k in range(1, 5):
+                want, _ = oracle.step_par(g.offsets, g.neighbors, want, policy=opts.get("policy", 0),
+                                          buffer_pow=opts.get("buffer_pow", 24))
+                p.run(k)
+                assert np.array_equal(p.get_labels(), want), f"{opts} iteration {k}"
