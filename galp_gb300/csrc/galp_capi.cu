@@ -112,11 +112,11 @@ void plan_chunk(const int64_t *off, int64_t v0, int64_t v1, ChunkPlan &P)
 
 }  // namespace
 
-constexpr int kMaxHubShift = 6;  // at most 64x the default hub partitions (and at most kHubMaxParts)
+constexpr int kMaxHubShift = 6;  // at most 64x the default hub partitions
 
 // Hash partitions of the big vertices: a hub of degree D gets ceil(D * 2^shift / 8192)
-// partitions, at most 2048 (its chunks emit at most D pairs, about 8192 per partition
-// while labels are still mostly distinct).  A partition holds 1.5x its share plus 256 pairs, plus one pair
+// partitions (its chunks emit at most D pairs, about 8192 per partition while labels are
+// still mostly distinct).  A partition holds 1.5x its share plus 256 pairs, plus one pair
 // per insert chunk of the hub: a label that appears in every chunk (late iterations) sends
 // all its pairs to one partition.  Partition indices are global; pair areas are relative
 // to the scope (out-of-core batches reuse one area).

@@ -213,7 +213,7 @@ struct Engine {
     bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
     bool symmetric = false;   // edge multiset symmetric (frontier marking along out-edges)
     Profiler prof;
-    galp_variant variant{0, 0.05f, 0.03f, 0, 0, 1, {}};  // kernel variant knobs (galp_set_variant)
+    galp_variant variant{0, 0.05f, 0.03f, 0, 0, 0, {}};  // kernel variant knobs (galp_set_variant)
     // out-of-core streaming
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};

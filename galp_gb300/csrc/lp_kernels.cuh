@@ -37,7 +37,7 @@ constexpr int kBigChunk = 1024;       // edges per big_insert CTA
 constexpr int kBigSlotChunk = 8192;   // distinct-list entries per big_stats CTA
 constexpr int kHubPartPairs = 8192;   // target pairs per hub partition (a hub of degree D: D / 8192 partitions)
 constexpr int kHubTab = 16384;        // shared-memory table slots of a hub partition (distinct labels < 16384)
-constexpr int kHubMaxParts = 2048;    // partitions of one hub at most (a chunk bins its pairs in shared memory)
+constexpr int kHubMaxParts = 1 << 20; // partitions of one hub at most
 constexpr int kHubCountThreads = 1024;
 constexpr int kHubBinMin = 256;       // a chunk with this many pairs bins them by partition in shared memory
 constexpr unsigned kFull = 0xFFFFFFFFu;
@@ -896,14 +896,12 @@ __device__ __forceinline__ uint32_t hub_part(uint32_t label, uint32_t nparts)
 // reservation per warp and partition; appends to a partition are contiguous, so its
 // sectors fill in L2).  A partition that is full drops the pair and flags the run, which
 // the host then redoes with twice the partitions.
-__global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
+__global__ void __launch_bounds__(kTB, 8) big_insert_kernel(IterArgs p)
 {
+    // 18 KB of shared memory: the rest of the unified L1 caches the label gathers
     __shared__ uint32_t skey[2 * kBigChunk];
     __shared__ uint32_t scnt[2 * kBigChunk];
     __shared__ uint16_t sused[kBigChunk];     // occupied local slots, compacted
-    __shared__ uint16_t spart[kBigChunk];     // partition of each compacted pair
-    __shared__ uint16_t srank[kBigChunk];     // its position among the chunk's pairs of that partition
-    __shared__ int sbin[kHubMaxParts];        // pairs per partition, then the partition's reserved base
     __shared__ int nused;
     if (!ctl_active(p.ctl)) return;
     if ((int)blockIdx.x >= p.nchunks) return;
@@ -961,18 +959,40 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
     __syncthreads();
     const int nloc = nused;
     const int q = p.hub_p0[bi];
-    const int np = p.hub_p0[bi + 1] - q;  // <= kHubMaxParts
+    const int np = p.hub_p0[bi + 1] - q;
     const int pcap = p.hub_pcap[bi];
     unsigned long long *area = p.pairs + p.hub_pbase[bi];
-    if (nloc >= kHubBinMin) {
+    if (nloc >= kHubBinMin && np <= kBigChunk) {
         // many pairs (labels still mostly distinct): bin them by partition, then one
-        // reservation per partition touched; the chunk's pairs of a partition land side by side
+        // reservation per partition touched; the chunk's pairs of a partition land side by
+        // side.  The pairs move to the front of the table arrays (nloc <= kBigChunk); the back
+        // halves then hold the bins (skey) and each pair's partition and rank (scnt).
+        constexpr int PAIRS = kBigChunk / kTB;
+        uint32_t kk[PAIRS], cc[PAIRS];
+#pragma unroll
+        for (int r = 0; r < PAIRS; ++r) {
+            const int i = threadIdx.x + r * kTB;
+            if (i < nloc) {
+                kk[r] = skey[sused[i]];
+                cc[r] = scnt[sused[i]];
+            }
+        }
+        __syncthreads();
+        int *sbin = reinterpret_cast<int *>(skey + kBigChunk);
+        uint32_t *spr = scnt + kBigChunk;  // partition << 16 | rank
+#pragma unroll
+        for (int r = 0; r < PAIRS; ++r) {
+            const int i = threadIdx.x + r * kTB;
+            if (i < nloc) {
+                skey[i] = kk[r];
+                scnt[i] = cc[r];
+            }
+        }
         for (int b = threadIdx.x; b < np; b += kTB) sbin[b] = 0;
         __syncthreads();
         for (int i = threadIdx.x; i < nloc; i += kTB) {
-            const int part = (int)hub_part(skey[sused[i]], (uint32_t)np);
-            spart[i] = (uint16_t)part;
-            srank[i] = (uint16_t)atomicAdd(&sbin[part], 1);
+            const uint32_t part = hub_part(skey[i], (uint32_t)np);
+            spr[i] = (part << 16) | (uint32_t)atomicAdd(&sbin[part], 1);
         }
         __syncthreads();
         for (int b = threadIdx.x; b < np; b += kTB) {
@@ -981,10 +1001,9 @@ __global__ void __launch_bounds__(kTB, 6) big_insert_kernel(IterArgs p)
         }
         __syncthreads();
         for (int i = threadIdx.x; i < nloc; i += kTB) {
-            const int part = spart[i];
-            const int at = sbin[part] + srank[i];
-            const uint32_t ls = sused[i];
-            if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)skey[ls] << 32) | scnt[ls];
+            const int part = (int)(spr[i] >> 16);
+            const int at = sbin[part] + (int)(spr[i] & 0xFFFFu);
+            if (at < pcap) area[(int64_t)part * pcap + at] = ((unsigned long long)skey[i] << 32) | scnt[i];
             else atomicOr(&p.ctl->err, kErrHubOverflow);
         }
         return;

@@ -65,7 +65,8 @@ typedef struct {
                                hash partitions (default 0); a partition that overflows makes the run
                                redo itself with the shift raised by one (up to 6) */
     int32_t cta_stage;      /* CTA counting of 257..2048 neighbours: 1 = the next vertex's neighbour IDs
-                               staged in shared memory by a bulk copy (default), 0 = global loads */
+                               staged in shared memory by a bulk copy, 0 = global loads (default: the
+                               stage takes unified L1 from the label gathers; 1.7x slower on R-MAT 26) */
     int32_t pad[2];
 } galp_variant;
 

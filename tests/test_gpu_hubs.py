@@ -117,7 +117,7 @@ def test_hubs_inside_out_of_core_batches(hub_graph, policy, bpow):
 
 @pytest.mark.parametrize("shift", [-6, 2])
 def test_hub_partition_count_does_not_change_labels(hub_graph, shift):
-    """Hubs count their labels in degree * 2^shift / 8192 hash partitions (at most 2048).
+    """Hubs count their labels in degree * 2^shift / 8192 hash partitions.
     With far too few partitions (shift -6: one per hub, whose table holds fewer distinct
     labels than the hub's neighbours carry) the first iterations overflow them; the run is
     redone with twice the partitions until none overflows, and its labels are exact.  More
