@@ -1509,6 +1509,25 @@ int galp_batch_tune(galp_ctx *ctx, int32_t niter, galp_tune_result *res)
         }
         *knob[k] = keep;
     }
+    // bucket shapes: the degree splits between warp and CTA counting (128 / 256) and
+    // between CTA sizes (1024 / 2048) and the insert aggregation, as fixed variant rows
+    // (frontier off); a row is kept only when it beats the per-iteration fixed rule by 1 %
+    int best_row = -1;
+    if (!rc && !E.frontier) {
+        const int mode0 = E.disp_mode, forced0 = E.disp_forced;
+        for (int row = 0; !rc && row < galp::kVar; row += 2) {
+            E.disp_mode = 2;
+            E.disp_forced = row;
+            float ms = 0.f;
+            rc = probe(ms);
+            if (!rc && ms < 0.99f * best_ms) {
+                best_ms = ms;
+                best_row = row;
+            }
+        }
+        E.disp_mode = best_row >= 0 ? 2 : mode0;
+        E.disp_forced = best_row >= 0 ? best_row : forced0;
+    }
     E.prof.on = was_on;
     E.prof.level = level;
     E.prof.spans[0].clear();
@@ -1527,6 +1546,7 @@ int galp_batch_tune(galp_ctx *ctx, int32_t niter, galp_tune_result *res)
         res->resolve_blocks_per_sm = E.resolve_bps;
         res->trials = trials;
         res->best_ms = best_ms;
+        res->dispatch_row = best_row;
     }
     return GALP_OK;
 }

@@ -294,7 +294,7 @@ class MLP:
 class TuneResult(ctypes.Structure):
     _fields_ = [("small_blocks_per_sm", ctypes.c_int32), ("mid_blocks_per_sm", ctypes.c_int32),
                 ("resolve_blocks_per_sm", ctypes.c_int32), ("trials", ctypes.c_int32), ("best_ms", ctypes.c_float),
-                ("pad", ctypes.c_int32)]
+                ("dispatch_row", ctypes.c_int32)]
 
 
 def batch_tune(batch, niter: int = 3) -> dict:
@@ -307,4 +307,5 @@ def batch_tune(batch, niter: int = 3) -> dict:
     if rc:
         raise RuntimeError(f"galp_batch_tune: {rc}")
     return dict(small_blocks_per_sm=r.small_blocks_per_sm, mid_blocks_per_sm=r.mid_blocks_per_sm,
-                resolve_blocks_per_sm=r.resolve_blocks_per_sm, trials=r.trials, best_ms=r.best_ms)
+                resolve_blocks_per_sm=r.resolve_blocks_per_sm, trials=r.trials, best_ms=r.best_ms,
+                dispatch_row=r.dispatch_row)

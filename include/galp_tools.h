@@ -86,7 +86,8 @@ typedef struct {
 typedef struct {
     int32_t small_blocks_per_sm, mid_blocks_per_sm, resolve_blocks_per_sm, trials;
     float best_ms;         /* probe run time with the chosen shapes */
-    int32_t pad;
+    int32_t dispatch_row;  /* bucket shapes: the variant row forced on every iteration (degree splits
+                              and insert aggregation), or -1 = the per-iteration fixed rule */
 } galp_tune_result;
 
 int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info);
@@ -95,7 +96,9 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info);
  * its label, with the loads of the counting kernels and no other work. */
 int galp_probe_gather(galp_ctx *ctx, int32_t reps, float *ms_per_pass);
 /* Launch-shape autotuner of a batched context (galp_batch_create): times probe runs of
- * niter iterations and keeps the fastest blocks-per-SM of the counting/resolve kernels. */
+ * niter iterations and keeps the fastest blocks-per-SM of the counting/resolve kernels,
+ * then the fastest bucket shapes (degree splits, insert aggregation) among the variant
+ * rows against the per-iteration fixed rule. */
 int galp_batch_tune(galp_ctx *ctx, int32_t niter, galp_tune_result *res);
 
 /* Per-iteration dispatch: mode 0 = fixed rule (default), 1 = learned MLP (weights: the

@@ -74,6 +74,7 @@ def test_repeat_runs_and_tuning_keep_labels():
         first = b.all_labels()
         res = b.tune(2)
         assert res["trials"] >= 4 and res["small_blocks_per_sm"] in (8, 16, 24, 32)
+        assert res["dispatch_row"] == -1 or res["dispatch_row"] in range(0, 16, 2)  # bucket shapes
         b.run(10)
         assert np.array_equal(b.all_labels(), first)
         b.run(4)  # another iteration count: a new captured graph
