@@ -155,6 +155,29 @@ def evaluate(g: Graph, w, niter: int = NITER, repeats: int = 3, frontier: int = 
     return out[0][0], out[1][0], out[1][1]
 
 
+def report(X, T, names, w=None) -> str:
+    """Markdown table: per training graph, the whole-run time of the fixed rule, of the
+    best row in every iteration (the most any per-iteration choice over this variant set
+    can gain) and of the learned rule (when weights are given)."""
+    idx = np.arange(len(T))
+    fixed = T[idx, fixed_rows(X)]
+    best = T.min(1)
+    learned = T[idx, predict_rows(w, X)] if w is not None else None
+    lines = ["| graph | fixed ms | best-per-iteration ms | fixed / best |" + (" learned ms | fixed / learned |" if w is not None else ""),
+             "|---|---:|---:|---:|" + ("---:|---:|" if w is not None else "")]
+    for name in dict.fromkeys(names.tolist()):
+        m = names == name
+        row = f"| {name} | {fixed[m].sum():.3f} | {best[m].sum():.3f} | {fixed[m].sum() / best[m].sum():.3f} |"
+        if learned is not None:
+            row += f" {learned[m].sum():.3f} | {fixed[m].sum() / learned[m].sum():.3f} |"
+        lines.append(row)
+    tot = f"| **all** | {fixed.sum():.3f} | {best.sum():.3f} | {fixed.sum() / best.sum():.3f} |"
+    if learned is not None:
+        tot += f" {learned.sum():.3f} | {fixed.sum() / learned.sum():.3f} |"
+    lines.append(tot)
+    return "\n".join(lines)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m galp_gb300.dispatch")
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -165,6 +188,9 @@ def main(argv=None):
     t.add_argument("--out", required=True)
     t.add_argument("--steps", type=int, default=1500)
     t.add_argument("--inc", action="store_true", help="also write csrc/dispatch_weights.inc")
+    r = sub.add_parser("report", help="fixed vs per-iteration best vs learned on a sweep")
+    r.add_argument("--data", required=True)
+    r.add_argument("--weights", default=None, help="weights .npy (default: none, no learned column)")
     e = sub.add_parser("evaluate")
     e.add_argument("--weights", required=True)
     e.add_argument("--rmat", type=int, default=20)
@@ -184,6 +210,9 @@ def main(argv=None):
               f"best {T.min(1).sum():.2f} ms")
         if a.inc:
             export_inc(w)
+    elif a.cmd == "report":
+        d = np.load(a.data)
+        print(report(d["X"], d["T"], d["names"], np.load(a.weights) if a.weights else None))
     else:
         w = np.load(a.weights)
         g = generate_rmat(a.rmat, 16, seed=3)
