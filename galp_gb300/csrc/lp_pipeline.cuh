@@ -151,6 +151,37 @@ __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t *l
     if (pred) list[base + __popc(m & ((1u << lane) - 1))] = value;
 }
 
+// Warp-private shared-memory buffer in front of a shared append-only list (the tied
+// lists): a warp appends with one ballot, and the buffer reaches the list with one global
+// atomic per kWarpBuf entries instead of one per append.  In the tie-heavy iterations
+// nearly every pack and vertex appends, and atomics on the one list counter serialise in L2.
+constexpr int kWarpBuf = 64;
+struct WarpBuf {
+    int32_t *buf;  // kWarpBuf entries of this warp's shared memory
+    int n = 0;     // warp-uniform fill
+    __device__ void flush(int32_t *list, int *ctr)
+    {
+        if (!n) return;
+        const int lane = threadIdx.x & 31;
+        int base = 0;
+        if (lane == 0) base = atomicAdd(ctr, n);
+        base = __shfl_sync(kFull, base, 0);
+        for (int i = lane; i < n; i += 32) list[base + i] = buf[i];
+        __syncwarp();
+        n = 0;
+    }
+    __device__ void append(bool pred, int32_t value, int32_t *list, int *ctr)
+    {
+        const unsigned m = __ballot_sync(kFull, pred);
+        if (!m) return;
+        if (n + __popc(m) > kWarpBuf) flush(list, ctr);
+        const int lane = threadIdx.x & 31;
+        if (pred) buf[n + __popc(m & ((1u << lane) - 1))] = value;
+        n += __popc(m);
+        __syncwarp();
+    }
+};
+
 // warp-level version of note_change (all lanes call it)
 __device__ __forceinline__ void warp_note_changes(const PipeArgs &p, bool changed, int32_t v)
 {
@@ -161,7 +192,7 @@ __device__ __forceinline__ void warp_note_changes(const PipeArgs &p, bool change
 // and move to the vertex lanes, which write the vertex state (all lanes call this).
 __device__ __forceinline__ void finish_small_pack(const PipeArgs &p, bool vl, int v, int deg, int pos, int d, int k,
                                                   int W, int cmin, int cmax, int rmin, int rmax,
-                                                  unsigned long long &changes)
+                                                  unsigned long long &changes, WarpBuf &tb)
 {
     const int lane = threadIdx.x & 31;
     // results live at each vertex's first slot lane; bring them to the vertex lanes
@@ -191,7 +222,7 @@ __device__ __forceinline__ void finish_small_pack(const PipeArgs &p, bool vl, in
             p.sm_r[v] = r0_v | (r1_v << 16);
         }
     }
-    warp_append(tied, v, p.tied_small, &p.ctl->tied_small);
+    tb.append(tied, v, p.tied_small, &p.ctl->tied_small);
     warp_note_changes(p, chg, v);
 }
 
@@ -200,12 +231,14 @@ __device__ __forceinline__ void finish_small_pack(const PipeArgs &p, bool vl, in
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256, 6) count_small_kernel(PipeArgs p)
 {
+    __shared__ int32_t tbuf[8][kWarpBuf];
     if (!ctl_active(p.ctl)) return;
     const bool fr = frontier_on(p);
     const int lane = threadIdx.x & 31;
     const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
     unsigned long long changes = 0;
+    WarpBuf tb{tbuf[threadIdx.x >> 5]};
     for (int pk = gw; pk < p.npacks; pk += nw) {
         const int v0 = p.pack_v0[pk], nv = p.pack_nv[pk];
         // vertex lanes: offsets, degrees, slot positions
@@ -217,7 +250,7 @@ __global__ void __launch_bounds__(256, 6) count_small_kernel(PipeArgs p)
             bool tied = false;
             if (vl && (__ldg(&p.off[v + 1]) > __ldg(&p.off[v]))) tied = (p.sm_kw[v] & 0xFFFF) > 1;
             if (vl && !tied) p.lab_out[v] = __ldg(&p.lab_in[v]);
-            warp_append(tied, v, p.tied_small, &p.ctl->tied_small);
+            tb.append(tied, v, p.tied_small, &p.ctl->tied_small);
             continue;
         }
         // The pack's CSR entries are contiguous: slot lane i holds entry obase + i.  Vertex
@@ -275,7 +308,7 @@ __global__ void __launch_bounds__(256, 6) count_small_kernel(PipeArgs p)
                 p.run_lab[e] = slab;
                 p.run_cnt[e] = (uint16_t)cnt;
             }
-            finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes);
+            finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes, tb);
             continue;
         }
         const unsigned eq = __match_any_sync(kFull, valid ? (uint32_t)lab : (0x80000000u | (uint32_t)lane)) & vm;
@@ -354,8 +387,9 @@ __global__ void __launch_bounds__(256, 6) count_small_kernel(PipeArgs p)
                 }
             }
         }
-        finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes);
+        finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes, tb);
     }
+    tb.flush(p.tied_small, &p.ctl->tied_small);
     flush_changes(changes, p.ctl);
 }
 
@@ -511,8 +545,9 @@ __device__ __forceinline__ bool use_aggregation(const PipeArgs &p, int v, int de
     return mode == 1 || (mode == 0 && 2 * p.dcnt[v] <= deg);
 }
 
-// Finish a counted vertex: per-vertex state, label or tied list.  One thread.
-__device__ __forceinline__ void finish_counted(const PipeArgs &p, int v, const Sum5 &s, int rmin, int rmax,
+// Finish a counted vertex: per-vertex state, and its label unless it is tied.  One
+// thread; returns whether the vertex is tied (the caller appends it to the tied list).
+__device__ __forceinline__ bool finish_counted(const PipeArgs &p, int v, const Sum5 &s, int rmin, int rmax,
                                                unsigned long long &changes)
 {
     p.dcnt[v] = s.d;
@@ -522,21 +557,41 @@ __device__ __forceinline__ void finish_counted(const PipeArgs &p, int v, const S
         p.lab_out[v] = s.mn;
         count_change(changes, s.mn, old);
         note_change(p, v, s.mn, old);
-    } else {
-        p.sm_c0[v] = s.mn;
-        p.sm_c1[v] = s.mx;
-        p.sm_r[v] = rmin | (rmax << 16);
-        p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
+        return false;
     }
+    p.sm_c0[v] = s.mn;
+    p.sm_c1[v] = s.mx;
+    p.sm_r[v] = rmin | (rmax << 16);
+    return true;
 }
 
 // Frontier: a clean vertex keeps its counts; it is re-resolved if tied, else keeps its
-// label.  One thread.
-__device__ __forceinline__ void carry_clean(const PipeArgs &p, int v)
+// label.  One thread; returns whether the vertex is tied.
+__device__ __forceinline__ bool carry_clean(const PipeArgs &p, int v)
 {
-    if ((p.sm_kw[v] & 0xFFFF) > 1) p.tied_mid[atomicAdd(&p.ctl->tied_mid, 1)] = v;
-    else p.lab_out[v] = __ldg(&p.lab_in[v]);
+    if ((p.sm_kw[v] & 0xFFFF) > 1) return true;
+    p.lab_out[v] = __ldg(&p.lab_in[v]);
+    return false;
 }
+
+// Thread-private buffer of one CTA's tied vertices (thread 0 finishes every vertex of a
+// CTA counting kernel): one list reservation per kWarpBuf vertices.
+struct ThreadBuf {
+    int32_t *buf;
+    int n = 0;
+    __device__ void flush(int32_t *list, int *ctr)
+    {
+        if (!n) return;
+        const int base = atomicAdd(ctr, n);
+        for (int i = 0; i < n; ++i) list[base + i] = buf[i];
+        n = 0;
+    }
+    __device__ void append(int32_t value, int32_t *list, int *ctr)
+    {
+        if (n == kWarpBuf) flush(list, ctr);
+        buf[n++] = value;
+    }
+};
 
 // One warp per mid vertex (33..256 neighbours): a 512-slot table of generation-tagged
 // 64-bit slots per warp (as the CTA tables: never cleared between vertices), probed over
@@ -545,6 +600,7 @@ __device__ __forceinline__ void carry_clean(const PipeArgs &p, int v)
 __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
 {
     __shared__ unsigned long long stab[kMidWarps][kMidSCap];
+    __shared__ int32_t tbuf[kMidWarps][kWarpBuf];
     if (!ctl_active(p.ctl)) return;
     const bool fr = frontier_on(p);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -552,6 +608,7 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
     const int nw = gridDim.x * kMidWarps;
     unsigned long long changes = 0;
     unsigned long long *tab = stab[w];
+    WarpBuf tb{tbuf[w]};
     for (int s = lane; s < kMidSCap; s += 32) tab[s] = 0ull;
     uint32_t gen = 0;
     __syncwarp();
@@ -559,7 +616,7 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
     for (int i = gw; i < nwarp_v; i += nw) {
         const int v = p.mid_v[i];
         if (fr && !p.dirty[v]) {
-            if (lane == 0) carry_clean(p, v);
+            tb.append(lane == 0 && carry_clean(p, v), v, p.tied_mid, &p.ctl->tied_mid);
             continue;
         }
         if (++gen > kT64GenMax) {
@@ -613,9 +670,11 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
                 }
             }
         }
-        if (lane == 0) finish_counted(p, v, sm, rmin, rmax, changes);
+        const bool tied = lane == 0 && finish_counted(p, v, sm, rmin, rmax, changes);
+        tb.append(tied, v, p.tied_mid, &p.ctl->tied_mid);
         __syncwarp();
     }
+    tb.flush(p.tied_mid, &p.ctl->tied_mid);
     flush_changes(changes, p.ctl);
 }
 
@@ -722,7 +781,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     __shared__ int sctr;
     __shared__ __align__(8) unsigned long long stage_bar;
     __shared__ int stage_ok;
+    __shared__ int32_t ctbuf[kWarpBuf];
     if (!ctl_active(p.ctl)) return;
+    ThreadBuf cb{ctbuf};  // thread 0's tied vertices
     // ranges of the degree-sorted mid list: 0 [pos1, pos_a), 1 [pos_a, pos2), 2 [pos2, pos_b),
     // 3 [pos_b, end)
     const DispatchState &ds = *p.disp;
@@ -759,7 +820,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         const int v = p.mid_v[first + i];
         if (fr && !p.dirty[v]) {
-            if (tid == 0) carry_clean(p, v);
+            if (tid == 0 && carry_clean(p, v)) cb.append(v, p.tied_mid, &p.ctl->tied_mid);
             continue;
         }
         if (++gen > kT64GenMax) {
@@ -823,9 +884,10 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
                           p.run_cnt + (o0 - p.nbr_shift), &sctr);
             }
         }
-        if (tid == 0) finish_counted(p, v, s, rmin, rmax, changes);
+        if (tid == 0 && finish_counted(p, v, s, rmin, rmax, changes)) cb.append(v, p.tied_mid, &p.ctl->tied_mid);
         __syncthreads();
     }
+    if (tid == 0) cb.flush(p.tied_mid, &p.ctl->tied_mid);
     // a copy that a wait gave up on still lands in this CTA's shared memory: wait for it
     // (bounded) before the CTA exits
     if (staged && lost_parity < 2) (void)mbar_wait(&stage_bar, lost_parity);
