@@ -156,7 +156,7 @@ __device__ __forceinline__ void warp_append(bool pred, int32_t value, int32_t *l
 // atomic per kWarpBuf entries instead of one per append.  In the tie-heavy iterations
 // nearly every pack and vertex appends, and atomics on the one list counter serialise in L2.
 constexpr int kWarpBuf = 64;
-constexpr int kSmallPipe = 2;  // small-vertex packs a warp loads together
+constexpr int kCtaBuf = 16;
 struct WarpBuf {
     int32_t *buf;  // kWarpBuf entries of this warp's shared memory
     int n = 0;     // warp-uniform fill
@@ -230,106 +230,57 @@ __device__ __forceinline__ void finish_small_pack(const PipeArgs &p, bool vl, in
 // ---------------------------------------------------------------------------
 // small vertices: one warp per pack
 // ---------------------------------------------------------------------------
-// One pack of small vertices, one warp: its vertices' offsets (ol: lane < nv holds the
-// offset of vertex v0 + lane, lane nv the pack's end; o32 the end when nv == 32) and every
-// slot lane's gathered label (lab_pre, for lanes below the pack's entry count) were loaded
-// by the caller, several packs at once.
-__device__ __forceinline__ void count_small_pack(const PipeArgs &p, bool fr, int v0, int nv, int64_t ol, int64_t o32,
-                                                 int lab_pre, unsigned long long &changes, WarpBuf &tb)
+__global__ void __launch_bounds__(256, 6) count_small_kernel(PipeArgs p)
 {
+    __shared__ int32_t tbuf[8][kWarpBuf];
+    if (!ctl_active(p.ctl)) return;
+    const bool fr = frontier_on(p);
     const int lane = threadIdx.x & 31;
-    // vertex lanes: offsets, degrees, slot positions
-    const bool vl = lane < nv;
-    const int v = v0 + lane;
-    if (fr && !__any_sync(kFull, vl && p.dirty[v])) {
-        // no label around this pack changed: counts and summaries carry over; labels
-        // of untied vertices stay, tied vertices are resolved again (run bases move)
-        bool tied = false;
-        if (vl && (__ldg(&p.off[v + 1]) > __ldg(&p.off[v]))) tied = (p.sm_kw[v] & 0xFFFF) > 1;
-        if (vl && !tied) p.lab_out[v] = __ldg(&p.lab_in[v]);
-        tb.append(tied, v, p.tied_small, &p.ctl->tied_small);
-        return;
-    }
-    // The pack's CSR entries are contiguous: slot lane i holds entry obase + i.  Vertex
-    // lanes read their offsets (an offset minus obase is the vertex's first slot lane);
-    // the slot lanes of one vertex form a segment [first, last] found from the mask of
-    // segment starts.
-    const int64_t obase = __shfl_sync(kFull, ol, 0);
-    const int64_t oend = nv < 32 ? __shfl_sync(kFull, ol, nv) : o32;
-    const int64_t onext = __shfl_down_sync(kFull, ol, 1);
-    const int deg = vl ? (int)((lane == 31 ? oend : onext) - ol) : 0;
-    const int pos = (int)(ol - obase);
-    const int total = (int)(oend - obase);
-    const bool valid = lane < total;
-    const unsigned starts = __reduce_or_sync(kFull, (vl && deg > 0) ? (1u << pos) : 0u);
-    const unsigned upto = (2u << lane) - 1u;  // lanes 0..lane
-    const int j = valid ? 31 - __clz(starts & upto) : lane;  // segment id = its first lane
-    const unsigned later_start = starts & ~upto;
-    const int seg_last = valid ? (later_start ? __ffs(later_start) - 2 : total - 1) : lane;
-    const int64_t oj = obase + j;  // the owner's first CSR entry
-    const int lab = valid ? lab_pre : 0;
-    const unsigned vm = valid ? (((seg_last == 31) ? kFull : ((2u << seg_last) - 1u)) & ~((1u << j) - 1u))
-                              : (1u << lane);
-    if (p.small_sort && p.lab27) {
-        // Sort-based counting: sort the pack by (vertex lane << 27 | label) in one 32-bit
-        // key (padding lanes last; a vertex keeps its slot lanes), then every run of equal
-        // keys is one distinct label: heads give d, run lengths give counts, and
-        // candidates come out in label order (cmin/cmax and their ranks by bit scans).
-        uint32_t sk = valid ? (((uint32_t)j << 27) | (uint32_t)lab) : 0xFFFFFFFFu;
-#pragma unroll
-        for (int kk = 2; kk <= 32; kk <<= 1) {
-#pragma unroll
-            for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-                const uint32_t ok = __shfl_xor_sync(kFull, sk, jj);
-                const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
-                sk = ((lower == up) ? (ok < sk) : (ok > sk)) ? ok : sk;
-            }
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long changes = 0;
+    WarpBuf tb{tbuf[threadIdx.x >> 5]};
+    for (int pk = gw; pk < p.npacks; pk += nw) {
+        const int v0 = p.pack_v0[pk], nv = p.pack_nv[pk];
+        // vertex lanes: offsets, degrees, slot positions
+        const bool vl = lane < nv;
+        const int v = v0 + lane;
+        if (fr && !__any_sync(kFull, vl && p.dirty[v])) {
+            // no label around this pack changed: counts and summaries carry over; labels
+            // of untied vertices stay, tied vertices are resolved again (run bases move)
+            bool tied = false;
+            if (vl && (__ldg(&p.off[v + 1]) > __ldg(&p.off[v]))) tied = (p.sm_kw[v] & 0xFFFF) > 1;
+            if (vl && !tied) p.lab_out[v] = __ldg(&p.lab_in[v]);
+            tb.append(tied, v, p.tied_small, &p.ctl->tied_small);
+            continue;
         }
-        const int first = __ffs(vm) - 1, last = 31 - __clz(vm);
-        const int slab = (int)(sk & ((1u << 27) - 1));
-        const uint32_t prevk = __shfl_up_sync(kFull, sk, 1);
-        const bool head = valid && (lane == first || prevk != sk);
-        const unsigned hm = __ballot_sync(kFull, head) & vm;
-        const unsigned later = hm & ~((2u << lane) - 1u);
-        const int cnt = head ? (later ? __ffs(later) - 1 : last + 1) - lane : 0;
-        const int W = seg_max(cnt, lane, first, last);
-        const unsigned cm = __ballot_sync(kFull, head && cnt == W) & vm;
-        const int k = __popc(cm), d = __popc(hm);
-        const int lo = cm ? __ffs(cm) - 1 : lane, hi = cm ? 31 - __clz(cm) : lane;
-        const int cmin = __shfl_sync(kFull, slab, lo), cmax = __shfl_sync(kFull, slab, hi);
-        const int rmin = __popc(hm & ((1u << lo) - 1)), rmax = __popc(hm & ((1u << hi) - 1));
-        if (head && k > 2) {
-            const int64_t e = oj - p.nbr_shift + __popc(hm & ((1u << lane) - 1));
-            p.run_lab[e] = slab;
-            p.run_cnt[e] = (uint16_t)cnt;
-        }
-        finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes, tb);
-        return;
-    }
-    const unsigned eq = __match_any_sync(kFull, valid ? (uint32_t)lab : (0x80000000u | (uint32_t)lane)) & vm;
-    const int cnt = __popc(eq);
-    const bool leader = valid && ((__ffs(eq) - 1) == lane);
-    const unsigned lm = __ballot_sync(kFull, leader);
-    const int first = __ffs(vm) - 1, last = 31 - __clz(vm);
-    const int W = seg_max(valid ? cnt : 0, lane, first, last);
-    const bool cand = leader && cnt == W;
-    const unsigned cm = __ballot_sync(kFull, cand);
-    const int k = __popc(cm & vm);
-    const int d = __popc(lm & vm);
-    int cmin, cmax, rmin = 0, rmax = 0;
-    if (__all_sync(kFull, !valid || k == 1)) {
-        const unsigned m = cm & vm;
-        cmin = cmax = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : lane);
-    } else {
-        cmin = seg_min(cand ? lab : INT_MAX, lane, first, last);
-        cmax = seg_max(cand ? lab : -1, lane, first, last);
-        rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
-        rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
-        if (p.lab27 && __any_sync(kFull, valid && k > 2)) {
-            // resolving a vertex with more than two candidates may need its runs in
-            // label order: sort the pack by (vertex lane << 27 | label) in one 32-bit
-            // key (labels below 2^27 - 1; padding lanes sort last), then spill the
-            // runs of those vertices; run lengths come from the run heads
+        // The pack's CSR entries are contiguous: slot lane i holds entry obase + i.  Vertex
+        // lanes read their offsets (an offset minus obase is the vertex's first slot lane);
+        // the slot lanes of one vertex form a segment [first, last] found from the mask of
+        // segment starts.
+        const int64_t ol = __ldg(&p.off[v0 + min(lane, nv)]);
+        const int64_t obase = __shfl_sync(kFull, ol, 0);
+        const int64_t oend = nv < 32 ? __shfl_sync(kFull, ol, nv) : __ldg(&p.off[v0 + 32]);
+        const int64_t onext = __shfl_down_sync(kFull, ol, 1);
+        const int deg = vl ? (int)((lane == 31 ? oend : onext) - ol) : 0;
+        const int pos = (int)(ol - obase);
+        const int total = (int)(oend - obase);
+        const bool valid = lane < total;
+        const unsigned starts = __reduce_or_sync(kFull, (vl && deg > 0) ? (1u << pos) : 0u);
+        const unsigned upto = (2u << lane) - 1u;  // lanes 0..lane
+        const int j = valid ? 31 - __clz(starts & upto) : lane;  // segment id = its first lane
+        const unsigned later_start = starts & ~upto;
+        const int seg_last = valid ? (later_start ? __ffs(later_start) - 2 : total - 1) : lane;
+        const int64_t oj = obase + j;  // the owner's first CSR entry
+        int lab = 0;
+        if (valid) lab = ld_label(&p.lab_in[ld_nbr(&p.nbr[obase + lane - p.nbr_shift])]);
+        const unsigned vm = valid ? (((seg_last == 31) ? kFull : ((2u << seg_last) - 1u)) & ~((1u << j) - 1u))
+                                  : (1u << lane);
+        if (p.small_sort && p.lab27) {
+            // Sort-based counting: sort the pack by (vertex lane << 27 | label) in one 32-bit
+            // key (padding lanes last; a vertex keeps its slot lanes), then every run of equal
+            // keys is one distinct label: heads give d, run lengths give counts, and
+            // candidates come out in label order (cmin/cmax and their ranks by bit scans).
             uint32_t sk = valid ? (((uint32_t)j << 27) | (uint32_t)lab) : 0xFFFFFFFFu;
 #pragma unroll
             for (int kk = 2; kk <= 32; kk <<= 1) {
@@ -340,90 +291,104 @@ __device__ __forceinline__ void count_small_pack(const PipeArgs &p, bool fr, int
                     sk = ((lower == up) ? (ok < sk) : (ok > sk)) ? ok : sk;
                 }
             }
+            const int first = __ffs(vm) - 1, last = 31 - __clz(vm);
             const int slab = (int)(sk & ((1u << 27) - 1));
             const uint32_t prevk = __shfl_up_sync(kFull, sk, 1);
             const bool head = valid && (lane == first || prevk != sk);
             const unsigned hm = __ballot_sync(kFull, head) & vm;
-            const int rank = __popc(hm & ((1u << lane) - 1));
             const unsigned later = hm & ~((2u << lane) - 1u);
-            const int sc = (later ? __ffs(later) - 1 : last + 1) - lane;
+            const int cnt = head ? (later ? __ffs(later) - 1 : last + 1) - lane : 0;
+            const int W = seg_max(cnt, lane, first, last);
+            const unsigned cm = __ballot_sync(kFull, head && cnt == W) & vm;
+            const int k = __popc(cm), d = __popc(hm);
+            const int lo = cm ? __ffs(cm) - 1 : lane, hi = cm ? 31 - __clz(cm) : lane;
+            const int cmin = __shfl_sync(kFull, slab, lo), cmax = __shfl_sync(kFull, slab, hi);
+            const int rmin = __popc(hm & ((1u << lo) - 1)), rmax = __popc(hm & ((1u << hi) - 1));
             if (head && k > 2) {
-                const int64_t e = oj - p.nbr_shift + rank;
+                const int64_t e = oj - p.nbr_shift + __popc(hm & ((1u << lane) - 1));
                 p.run_lab[e] = slab;
-                p.run_cnt[e] = (uint16_t)sc;
+                p.run_cnt[e] = (uint16_t)cnt;
             }
-        } else if (__any_sync(kFull, valid && k > 2)) {
-            // labels of 27 bits or more: 64-bit (vertex, label) keys
-            unsigned long long sk =
-                valid ? (((unsigned long long)(unsigned)j << 32) | (unsigned)lab) : (0xFFFFFFFF00000000ull | lane);
-            int sc = valid ? cnt : 0;
+            finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes, tb);
+            continue;
+        }
+        const unsigned eq = __match_any_sync(kFull, valid ? (uint32_t)lab : (0x80000000u | (uint32_t)lane)) & vm;
+        const int cnt = __popc(eq);
+        const bool leader = valid && ((__ffs(eq) - 1) == lane);
+        const unsigned lm = __ballot_sync(kFull, leader);
+        const int first = __ffs(vm) - 1, last = 31 - __clz(vm);
+        const int W = seg_max(valid ? cnt : 0, lane, first, last);
+        const bool cand = leader && cnt == W;
+        const unsigned cm = __ballot_sync(kFull, cand);
+        const int k = __popc(cm & vm);
+        const int d = __popc(lm & vm);
+        int cmin, cmax, rmin = 0, rmax = 0;
+        if (__all_sync(kFull, !valid || k == 1)) {
+            const unsigned m = cm & vm;
+            cmin = cmax = __shfl_sync(kFull, lab, m ? (__ffs(m) - 1) : lane);
+        } else {
+            cmin = seg_min(cand ? lab : INT_MAX, lane, first, last);
+            cmax = seg_max(cand ? lab : -1, lane, first, last);
+            rmin = __popc(__ballot_sync(kFull, leader && lab < cmin) & vm);
+            rmax = __popc(__ballot_sync(kFull, leader && lab < cmax) & vm);
+            if (p.lab27 && __any_sync(kFull, valid && k > 2)) {
+                // resolving a vertex with more than two candidates may need its runs in
+                // label order: sort the pack by (vertex lane << 27 | label) in one 32-bit
+                // key (labels below 2^27 - 1; padding lanes sort last), then spill the
+                // runs of those vertices; run lengths come from the run heads
+                uint32_t sk = valid ? (((uint32_t)j << 27) | (uint32_t)lab) : 0xFFFFFFFFu;
 #pragma unroll
-            for (int kk = 2; kk <= 32; kk <<= 1) {
+                for (int kk = 2; kk <= 32; kk <<= 1) {
 #pragma unroll
-                for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-                    const unsigned long long ok = __shfl_xor_sync(kFull, sk, jj);
-                    const int oc = __shfl_xor_sync(kFull, sc, jj);
-                    const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
-                    if ((lower == up) ? (ok < sk) : (ok > sk)) {
-                        sk = ok;
-                        sc = oc;
+                    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                        const uint32_t ok = __shfl_xor_sync(kFull, sk, jj);
+                        const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
+                        sk = ((lower == up) ? (ok < sk) : (ok > sk)) ? ok : sk;
                     }
                 }
+                const int slab = (int)(sk & ((1u << 27) - 1));
+                const uint32_t prevk = __shfl_up_sync(kFull, sk, 1);
+                const bool head = valid && (lane == first || prevk != sk);
+                const unsigned hm = __ballot_sync(kFull, head) & vm;
+                const int rank = __popc(hm & ((1u << lane) - 1));
+                const unsigned later = hm & ~((2u << lane) - 1u);
+                const int sc = (later ? __ffs(later) - 1 : last + 1) - lane;
+                if (head && k > 2) {
+                    const int64_t e = oj - p.nbr_shift + rank;
+                    p.run_lab[e] = slab;
+                    p.run_cnt[e] = (uint16_t)sc;
+                }
+            } else if (__any_sync(kFull, valid && k > 2)) {
+                // labels of 27 bits or more: 64-bit (vertex, label) keys
+                unsigned long long sk =
+                    valid ? (((unsigned long long)(unsigned)j << 32) | (unsigned)lab) : (0xFFFFFFFF00000000ull | lane);
+                int sc = valid ? cnt : 0;
+#pragma unroll
+                for (int kk = 2; kk <= 32; kk <<= 1) {
+#pragma unroll
+                    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+                        const unsigned long long ok = __shfl_xor_sync(kFull, sk, jj);
+                        const int oc = __shfl_xor_sync(kFull, sc, jj);
+                        const bool up = (lane & kk) == 0, lower = (lane & jj) == 0;
+                        if ((lower == up) ? (ok < sk) : (ok > sk)) {
+                            sk = ok;
+                            sc = oc;
+                        }
+                    }
+                }
+                const int slab = (int)(unsigned)sk;
+                const int prev = __shfl_up_sync(kFull, slab, 1);
+                const bool head = valid && (lane == first || prev != slab);
+                const unsigned hm = __ballot_sync(kFull, head) & vm;
+                const int rank = __popc(hm & ((1u << lane) - 1));
+                if (head && k > 2) {
+                    const int64_t e = oj - p.nbr_shift + rank;
+                    p.run_lab[e] = slab;
+                    p.run_cnt[e] = (uint16_t)sc;
+                }
             }
-            const int slab = (int)(unsigned)sk;
-            const int prev = __shfl_up_sync(kFull, slab, 1);
-            const bool head = valid && (lane == first || prev != slab);
-            const unsigned hm = __ballot_sync(kFull, head) & vm;
-            const int rank = __popc(hm & ((1u << lane) - 1));
-            if (head && k > 2) {
-                const int64_t e = oj - p.nbr_shift + rank;
-                p.run_lab[e] = slab;
-                p.run_cnt[e] = (uint16_t)sc;
-            }
         }
-    }
-    finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes, tb);
-}
-
-__global__ void __launch_bounds__(256, 5) count_small_kernel(PipeArgs p)
-{
-    __shared__ int32_t tbuf[8][kWarpBuf];
-    if (!ctl_active(p.ctl)) return;
-    const bool fr = frontier_on(p);
-    const int lane = threadIdx.x & 31;
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nw = (gridDim.x * blockDim.x) >> 5;
-    unsigned long long changes = 0;
-    WarpBuf tb{tbuf[threadIdx.x >> 5]};
-    // Packs are taken kSmallPipe at a time: their pack records, offsets, neighbour IDs and
-    // labels are loaded stage by stage for all of them, so one memory round trip of each
-    // dependent stage serves several packs.
-    for (int pk0 = gw; pk0 < p.npacks; pk0 += kSmallPipe * nw) {
-        int v0s[kSmallPipe], nvs[kSmallPipe], labs[kSmallPipe];
-        int64_t ols[kSmallPipe], o32s[kSmallPipe];
-#pragma unroll
-        for (int u = 0; u < kSmallPipe; ++u) {
-            const int pk = pk0 + u * nw;
-            v0s[u] = pk < p.npacks ? p.pack_v0[pk] : 0;
-            nvs[u] = pk < p.npacks ? (int)p.pack_nv[pk] : 0;
-        }
-#pragma unroll
-        for (int u = 0; u < kSmallPipe; ++u) {
-            ols[u] = nvs[u] ? __ldg(&p.off[v0s[u] + min(lane, nvs[u])]) : 0;
-            o32s[u] = nvs[u] == 32 ? __ldg(&p.off[v0s[u] + 32]) : 0;
-        }
-        int nbs[kSmallPipe];
-#pragma unroll
-        for (int u = 0; u < kSmallPipe; ++u) {
-            const int64_t obase = __shfl_sync(kFull, ols[u], 0);
-            const int64_t oend = nvs[u] < 32 ? __shfl_sync(kFull, ols[u], nvs[u]) : o32s[u];
-            nbs[u] = (nvs[u] && lane < (int)(oend - obase)) ? ld_nbr(&p.nbr[obase + lane - p.nbr_shift]) : -1;
-        }
-#pragma unroll
-        for (int u = 0; u < kSmallPipe; ++u) labs[u] = nbs[u] >= 0 ? ld_label(&p.lab_in[nbs[u]]) : 0;
-#pragma unroll
-        for (int u = 0; u < kSmallPipe; ++u)
-            if (nvs[u]) count_small_pack(p, fr, v0s[u], nvs[u], ols[u], o32s[u], labs[u], changes, tb);
+        finish_small_pack(p, vl, v, deg, pos, d, k, W, cmin, cmax, rmin, rmax, changes, tb);
     }
     tb.flush(p.tied_small, &p.ctl->tied_small);
     flush_changes(changes, p.ctl);
@@ -611,8 +576,10 @@ __device__ __forceinline__ bool carry_clean(const PipeArgs &p, int v)
 }
 
 // One thread's buffer of tied vertices in shared memory (thread 0 finishes every vertex of
-// a CTA counting kernel): one list reservation per kWarpBuf vertices.  Buffer and fill
-// live in shared memory, so the CTA's other threads carry no registers for it.
+// a CTA counting kernel): one list reservation per kCtaBuf vertices.  Buffer and fill
+// live in shared memory, so the CTA's other threads carry no registers for it; 16 entries
+// keep two 96 KB-table CTAs inside the 196 KB shared-memory carve-out (more would leave
+// the label gathers almost no L1).
 __device__ __forceinline__ void tbuf_flush(int32_t *buf, int *n, int32_t *list, int *ctr)
 {
     const int c = *n;
@@ -624,7 +591,7 @@ __device__ __forceinline__ void tbuf_flush(int32_t *buf, int *n, int32_t *list, 
 
 __device__ __forceinline__ void tbuf_append(int32_t *buf, int *n, int32_t value, int32_t *list, int *ctr)
 {
-    if (*n == kWarpBuf) tbuf_flush(buf, n, list, ctr);
+    if (*n == kCtaBuf) tbuf_flush(buf, n, list, ctr);
     buf[(*n)++] = value;
 }
 
@@ -816,7 +783,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     __shared__ int sctr;
     __shared__ __align__(8) unsigned long long stage_bar;
     __shared__ int stage_ok;
-    __shared__ int32_t ctbuf[kWarpBuf];  // thread 0's tied vertices
+    __shared__ int32_t ctbuf[kCtaBuf];  // thread 0's tied vertices
     __shared__ int ctn;
     if (!ctl_active(p.ctl)) return;
     if (threadIdx.x == 0) ctn = 0;  // ordered before thread 0's own uses
