@@ -105,8 +105,8 @@ def test_dispatch_set_validates():
 
 def test_builtin_learned_dispatch_is_exact_and_not_slower():
     """opts.dispatch = 1 loads the network trained on this machine's timing sweeps; it
-    changes only speed.  Per-iteration device time against the fixed rule is printed;
-    the bound allows run-to-run noise."""
+    changes only speed, and must not make a run slower than the fixed rule (2 % allowance
+    for run-to-run noise of the best of three runs per iteration)."""
     g = galp_gb300.generate_rmat(19, 32, a=0.5, b=0.1667, c=0.1667, seed=9)
     times = {}
     labels = {}
@@ -125,4 +125,4 @@ def test_builtin_learned_dispatch_is_exact_and_not_slower():
     assert np.array_equal(labels["fixed"], labels["learned"])
     print(f"fixed {times['fixed']:.3f} ms, learned {times['learned']:.3f} ms, "
           f"gain {times['fixed'] / times['learned']:.3f}x")
-    assert times["learned"] <= 1.10 * times["fixed"]
+    assert times["learned"] <= 1.02 * times["fixed"]
