@@ -169,6 +169,7 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
         sc.e0 = off[sc.v0];
         sc.e1 = off[sc.v1];
         sc.p0 = (int32_t)S.pack_v0.size();
+        sc.sv0 = (int32_t)S.small_v.size();
         sc.m0 = (int32_t)S.mid_v.size();
         sc.b0 = (int32_t)S.big_v.size();
         sc.c0 = (int32_t)S.chunk_big.size();
@@ -223,15 +224,19 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             sc.nml = (int32_t)(upto_large - upto_mid);
             sc.nmx = (int32_t)(total - upto_large);
         }
+        const size_t sb = S.small_v.size();
         S.pack_v0.resize(pb + np);
         S.pack_nv.resize(pb + np);
+        S.small_v.resize(sb + (size_t)nsmall);
         S.mid_v.resize(mb + nm);
         S.mid_deg.resize(mb + nm);
         {
-            auto place = [&](int t, size_t p0) {
+            auto place = [&](int t, size_t p0, size_t s0) {
                 ChunkPlan &P = plans[(size_t)t];
                 std::copy(P.pack_v0.begin(), P.pack_v0.end(), S.pack_v0.begin() + (ptrdiff_t)p0);
                 std::copy(P.pack_nv.begin(), P.pack_nv.end(), S.pack_nv.begin() + (ptrdiff_t)p0);
+                for (size_t k2 = 0; k2 < P.pack_v0.size(); ++k2)
+                    for (int u = 0; u < P.pack_nv[k2]; ++u) S.small_v[s0++] = P.pack_v0[k2] + u;
                 for (size_t i = 0; i < P.mid.size(); ++i) {
                     const size_t at = (size_t)P.mid_count[(size_t)P.mid_deg[i]]++;
                     S.mid_v[at] = P.mid[i];
@@ -239,11 +244,12 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
                 }
             };
             std::vector<std::thread> th;
-            size_t p0 = pb;
+            size_t p0 = pb, s0 = sb;
             for (int t = 0; t < T; ++t) {
-                if (T == 1) place(t, p0);
-                else th.emplace_back(place, t, p0);
+                if (T == 1) place(t, p0, s0);
+                else th.emplace_back(place, t, p0, s0);
                 p0 += plans[(size_t)t].pack_v0.size();
+                s0 += (size_t)plans[(size_t)t].nsmall;
             }
             for (auto &x : th) x.join();
         }
@@ -268,6 +274,7 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             S.m_big += deg;
         }
         sc.np = (int32_t)S.pack_v0.size() - sc.p0;
+        sc.nsv = (int32_t)S.small_v.size() - sc.sv0;
         sc.nb = (int32_t)S.big_v.size() - sc.b0;
         sc.nc = (int32_t)S.chunk_big.size() - sc.c0;
         sc.ns = (int32_t)S.schunk_big.size() - sc.s0;
@@ -390,6 +397,7 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     int rc;
     if ((rc = upload(b_pack_v0, d_pack_v0, sched.pack_v0, st, h2d))) return rc;
     if ((rc = upload(b_pack_nv, d_pack_nv, sched.pack_nv, st, h2d))) return rc;
+    if ((rc = upload(b_small_v, d_small_v, sched.small_v, st, h2d))) return rc;
     if ((rc = upload(b_mid_v, d_mid_v, sched.mid_v, st, h2d))) return rc;
     if ((rc = upload(b_big_v, d_big_v, sched.big_v, st, h2d))) return rc;
     if ((rc = upload(b_big_ooff, d_big_ooff, sched.big_ooff, st, h2d))) return rc;
@@ -661,6 +669,8 @@ PipeArgs Engine::pipe_args(const Scope &sc) const
     q.pack_v0 = d_pack_v0 + sc.p0;
     q.pack_nv = d_pack_nv + sc.p0;
     q.npacks = sc.np;
+    q.small_v = d_small_v + sc.sv0;
+    q.nsmall = sc.nsv;
     q.mid_v = d_mid_v + sc.m0;
     q.nmid_s = sc.nms;
     q.nmid_l = sc.nml;
@@ -732,7 +742,12 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         if (prof.on) prof.spans[1].push_back({e0, prof.mark(st)});
     }
     if (prof.on) e0 = prof.mark(st);
-    if (q.npacks) {
+    if (q.npacks && variant.small_sort == 2) {
+        // one thread per small vertex, over the small-vertex list
+        const int blocks = (int)std::min<int64_t>(((int64_t)q.nsmall + 127) / 128, (int64_t)sms * kSmallLaneBlocks);
+        count_small_lane_kernel<<<blocks, 128, 0, st>>>(q);
+        launched("count_small_lane_kernel", st);
+    } else if (q.npacks) {
         // several waves: blocks that finish early take up the remaining ones (pack costs vary)
         const int blocks = (int)std::min<int64_t>(((int64_t)q.npacks * 32 + 255) / 256, (int64_t)sms * small_bps);
         count_small_kernel<<<blocks, 256, 0, st>>>(q);
@@ -1294,7 +1309,7 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
 int galp_set_variant(galp_ctx *ctx, const galp_variant *v)
 {
     if (!ctx || !v || v->agg_mode < 0 || v->agg_mode > 2 || !(v->frontier_frac >= 0.f && v->frontier_frac <= 1.f) ||
-        !(v->learned_margin >= 0.f && v->learned_margin < 10.f) || v->small_sort < 0 || v->small_sort > 1 ||
+        !(v->learned_margin >= 0.f && v->learned_margin < 10.f) || v->small_sort < 0 || v->small_sort > 2 ||
         v->cta_stage < 0 || v->cta_stage > 1)
         return GALP_EINVAL;
     if (v->hub_part_shift < -16 || v->hub_part_shift > kMaxHubShift) return GALP_EINVAL;
@@ -1305,6 +1320,10 @@ int galp_set_variant(galp_ctx *ctx, const galp_variant *v)
         if (rc) return rc;
     }
     ctx->eng.variant = *v;
+    // a batched run is a captured CUDA graph: capture again with the new kernels
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+    ctx->graph_iters = -1;
     return GALP_OK;
 }
 

@@ -53,6 +53,7 @@ struct Scope {
     int32_t b0 = 0, nb = 0;    // big vertices
     int32_t c0 = 0, nc = 0;    // big insert chunks
     int32_t s0 = 0, ns = 0;    // big stats chunks
+    int32_t sv0 = 0, nsv = 0;  // vertices of degree <= 32 (small_v), in vertex order
     int32_t last_v = -1;       // last vertex of the scope that owns runs
     int32_t q0 = 0, nq = 0;    // hash partitions of the scope's big vertices
     int64_t pair_slots = 0;    // pair area of those partitions
@@ -63,6 +64,7 @@ struct Scope {
 struct Schedule {
     std::vector<int32_t> pack_v0;    // first vertex of each pack (<= 32 vertices, <= 32 edges)
     std::vector<uint8_t> pack_nv;    // vertices in each pack
+    std::vector<int32_t> small_v;    // per scope: the pack vertices one by one, in vertex order
     std::vector<int32_t> mid_v;      // per scope: mid, large and xl vertices in ascending degree
     std::vector<int32_t> mid_deg;    // degree of each mid_v entry
     std::vector<int32_t> big_v;      // vertex of each big entry
@@ -185,7 +187,7 @@ struct Engine {
     const int32_t *h_nbr = nullptr;  // caller's host neighbours (streamed for policies 1/2)
     bool registered = false;         // the library pinned h_nbr
     Schedule sched;
-    DevBuf b_nbr[2], b_off, b_pack_v0, b_pack_nv, b_mid_v, b_big_v;
+    DevBuf b_nbr[2], b_off, b_pack_v0, b_pack_nv, b_small_v, b_mid_v, b_big_v;
     DevBuf b_chunk_big, b_chunk_e0, b_chunk_e1, b_schunk_big, b_schunk_s0, b_schunk_s1, b_big_ooff;
     DevBuf b_hub_p0, b_hub_pbase, b_hub_pcap, b_part_big, b_pfill, b_psum, b_pairs, b_big_list;
     DevBuf b_lab0, b_lab1, b_ctl, b_bstat, b_big_a, b_bad;
@@ -200,6 +202,7 @@ struct Engine {
     bool frontier = false;             // requested, policy 0, and the graph is symmetric
     int32_t *d_pack_v0 = nullptr;
     uint8_t *d_pack_nv = nullptr;
+    int32_t *d_small_v = nullptr;
     int32_t *d_mid_v = nullptr;
     int32_t *d_big_v = nullptr;
     int64_t *d_big_ooff = nullptr;

@@ -54,6 +54,8 @@ struct PipeArgs {
     const int32_t *pack_v0;
     const uint8_t *pack_nv;
     int32_t npacks;
+    const int32_t *small_v; // the same vertices one by one (thread-per-vertex counting)
+    int32_t nsmall;
     const int32_t *mid_v;   // mid (33..256), then large (257..2048), then xl (2049..12288) vertices
     int32_t nmid_s, nmid_l, nmid_x;
     // per-vertex state (global vertex index)
@@ -84,7 +86,8 @@ struct PipeArgs {
     const int32_t *gid;     // graph of every vertex
     int32_t ngraphs;
     int32_t lab27;          // every label below 2^27 - 1 (32-bit sort keys in packs)
-    int32_t small_sort;     // small packs: sort-based counting (needs lab27) instead of match_any
+    int32_t small_sort;     // small vertices: 0 match-based packs, 1 sort-based packs (needs lab27),
+                            // 2 one thread per vertex
 };
 
 // Graph of vertex v in batched mode: the largest g with g_v0[g] <= v.
@@ -593,6 +596,121 @@ __device__ __forceinline__ void tbuf_append(int32_t *buf, int *n, int32_t value,
 {
     if (*n == kCtaBuf) tbuf_flush(buf, n, list, ctr);
     buf[(*n)++] = value;
+}
+
+// Small vertices (at most 32 neighbours), one thread each (`small_sort` 2): a vertex's
+// neighbour labels go to the thread's 32-entry row of shared memory (element j of lane l at
+// l * 32 + (j ^ l): the lanes' rows are bank-disjoint), are sorted there by insertion, and
+// one pass over the sorted row gives the distinct count, the runs' counts, the maximum, the
+// candidates and the ranks of the smallest and largest candidate; vertices with more than
+// two candidates spill their runs in label order, as the pack kernel does.  Against the
+// warp-per-pack kernel this spends per vertex a few instructions per neighbour instead of
+// the per-pack segment masks, matches and segmented shuffles.
+constexpr int kSmallLaneBlocks = 8;  // resident 128-thread blocks per SM (16 KB of rows each)
+__global__ void __launch_bounds__(128, kSmallLaneBlocks) count_small_lane_kernel(PipeArgs p)
+{
+    __shared__ int32_t rows[4][32 * 32];
+    __shared__ int32_t tbuf[4][kWarpBuf];
+    if (!ctl_active(p.ctl)) return;
+    const bool fr = frontier_on(p);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t *row = rows[w] + lane * 32;
+    WarpBuf tb{tbuf[w]};
+    unsigned long long changes = 0;
+    const int stride = gridDim.x * 128;
+    // warp-uniform trip count: every lane runs the loop the same number of times
+    for (int base = blockIdx.x * 128 + w * 32; base < p.nsmall; base += stride) {
+        const int i = base + lane;
+        const bool active = i < p.nsmall;
+        const int v = active ? p.small_v[i] : 0;
+        bool tied = false, chg = false;
+        if (active) {
+            const int64_t o0 = __ldg(&p.off[v]);
+            const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
+            const int32_t old = __ldg(&p.lab_in[v]);
+            if (fr && !p.dirty[v]) {
+                // no label around the vertex changed: its counts carry over
+                tied = deg > 0 && (p.sm_kw[v] & 0xFFFF) > 1;
+                if (!tied) p.lab_out[v] = old;
+            } else if (deg == 0) {
+                p.dcnt[v] = 0;
+                p.lab_out[v] = old;
+            } else {
+                const int32_t *nb = p.nbr + (o0 - p.nbr_shift);
+                // gather: all of the vertex's neighbour IDs, then all its labels, in flight
+                int ids[4];
+                int j = 0;
+                for (; j + 4 <= deg; j += 4) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) ids[u] = __ldg(&nb[j + u]);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) row[(j + u) ^ lane] = ld_label(&p.lab_in[ids[u]]);
+                }
+                for (; j < deg; ++j) row[j ^ lane] = ld_label(&p.lab_in[__ldg(&nb[j])]);
+                // insertion sort of the row
+                for (int a = 1; a < deg; ++a) {
+                    const int32_t x = row[a ^ lane];
+                    int b = a - 1;
+                    while (b >= 0 && row[b ^ lane] > x) {
+                        row[(b + 1) ^ lane] = row[b ^ lane];
+                        --b;
+                    }
+                    row[(b + 1) ^ lane] = x;
+                }
+                // runs
+                int d = 0, W = 0, k = 0, rmin = 0, rmax = 0;
+                int32_t cmin = 0, cmax = 0;
+                for (int a = 0; a < deg;) {
+                    const int32_t lab = row[a ^ lane];
+                    int e = a + 1;
+                    while (e < deg && row[e ^ lane] == lab) ++e;
+                    const int c = e - a;
+                    if (c > W) {
+                        W = c;
+                        k = 1;
+                        cmin = cmax = lab;
+                        rmin = rmax = d;
+                    } else if (c == W) {
+                        ++k;
+                        cmax = lab;
+                        rmax = d;
+                    }
+                    ++d;
+                    a = e;
+                }
+                if (k > 2) {  // resolving may need the runs: spill them in label order
+                    int32_t *rl = p.run_lab + (o0 - p.nbr_shift);
+                    uint16_t *rc = p.run_cnt + (o0 - p.nbr_shift);
+                    int r = 0;
+                    for (int a = 0; a < deg;) {
+                        const int32_t lab = row[a ^ lane];
+                        int e = a + 1;
+                        while (e < deg && row[e ^ lane] == lab) ++e;
+                        rl[r] = lab;
+                        rc[r] = (uint16_t)(e - a);
+                        ++r;
+                        a = e;
+                    }
+                }
+                p.dcnt[v] = d;
+                p.sm_kw[v] = k | (W << 16);
+                if (k == 1) {
+                    p.lab_out[v] = cmin;
+                    count_change(changes, cmin, old);
+                    chg = cmin != old;
+                } else {
+                    tied = true;
+                    p.sm_c0[v] = cmin;
+                    p.sm_c1[v] = cmax;
+                    p.sm_r[v] = rmin | (rmax << 16);
+                }
+            }
+        }
+        tb.append(tied, v, p.tied_small, &p.ctl->tied_small);
+        warp_note_changes(p, chg, v);
+    }
+    tb.flush(p.tied_small, &p.ctl->tied_small);
+    flush_changes(changes, p.ctl);
 }
 
 // One warp per mid vertex (33..256 neighbours): a 512-slot table of generation-tagged

@@ -124,3 +124,20 @@ def test_hub_vertices_are_not_supported_in_batches():
     with pytest.raises(galp_gb300.GalpError) as e:
         galp_gb300.Batch([g, galp_gb300.generate_sbm([64] * 4, 6.0, 1.0, seed=1)])
     assert e.value.code == -6
+
+
+def test_thread_per_vertex_small_counting_in_batches():
+    # small_sort = 2 (one thread per small vertex) inside a captured batched run: every
+    # graph keeps its standalone labels, iteration count and change counts
+    from galp_gb300 import tools
+
+    graphs = _mixed_graphs(12, seed=11)
+    with galp_gb300.Batch(graphs) as b:
+        b.run(10)
+        first = b.all_labels()
+        tools.set_variant(b, small_sort=2)
+        b.run(10)
+        assert np.array_equal(b.all_labels(), first)
+        for i, g in enumerate(graphs):
+            it, want, counts = oracle.run(g.offsets, g.neighbors, 10)
+            assert b.graph_stats(i) == (it, list(counts))

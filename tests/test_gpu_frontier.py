@@ -159,14 +159,39 @@ def test_insert_aggregation_variants(agg):
     assert its == it and np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("small_sort", [0, 1])
+@pytest.mark.parametrize("small_sort", [0, 1, 2])
 def test_small_pack_counting_variants(small_sort):
-    # sort-based and match-based counting of small-vertex packs give the same labels
+    # sort-based and match-based counting of small-vertex packs, and one thread per small
+    # vertex, give the same labels, with the frontier too
     for g in (galp_gb300.generate_rmat(16, 8, seed=6), galp_gb300.generate_lfr(20000, seed=8),
               galp_gb300.generate_sbm([128] * 32, 10.0, 3.0, seed=2)):
-        with galp_gb300.Propagator(g) as p:
+        it, want, counts = oracle.run(g.offsets, g.neighbors, 10)
+        for fr in (0, 1):
+            with galp_gb300.Propagator(g, frontier=fr) as p:
+                tools.set_variant(p, small_sort=small_sort)
+                p.run(10)
+                got, its, upd = p.get_labels(), p.iters_run, list(p.updates)
+            assert its == it and upd == list(counts) and np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("small_sort", [0, 2])
+def test_small_counting_variants_out_of_core_and_isolated(small_sort):
+    # isolated vertices among the small ones, and out-of-core batches (small-vertex lists
+    # per batch)
+    g = galp_gb300.generate_sbm([64] * 16, 8.0, 2.0, seed=9)
+    new_n = g.n + 4
+    iso = np.array([0, 3, 500, new_n - 1])
+    keep = np.setdiff1d(np.arange(new_n), iso)
+    deg = np.zeros(new_n, np.int64)
+    deg[keep] = g.degrees()
+    off = np.zeros(new_n + 1, np.int64)
+    off[1:] = np.cumsum(deg)
+    g2 = galp_gb300.Graph(off, keep[g.neighbors].astype(np.int32))
+    for opts in ({}, {"policy": 2, "buffer_pow": 11}):
+        it, want, counts = oracle.run(g2.offsets, g2.neighbors, 10, policy=opts.get("policy", 0),
+                                      buffer_pow=opts.get("buffer_pow", 24))
+        with galp_gb300.Propagator(g2, **opts) as p:
             tools.set_variant(p, small_sort=small_sort)
             p.run(10)
-            got, its, upd = p.get_labels(), p.iters_run, list(p.updates)
-        it, want, counts = oracle.run(g.offsets, g.neighbors, 10)
-        assert its == it and upd == list(counts) and np.array_equal(got, want)
+            assert p.iters_run == it and list(p.updates) == list(counts)
+            assert np.array_equal(p.get_labels(), want)
