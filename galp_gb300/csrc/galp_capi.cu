@@ -253,6 +253,8 @@ bool build_schedule(Schedule &S, int64_t n, const int64_t *off, const std::vecto
             }
             for (auto &x : th) x.join();
         }
+        sc.nnarrow = (int32_t)(std::upper_bound(S.mid_deg.begin() + (ptrdiff_t)mb, S.mid_deg.end(), kNarrowMax) -
+                               (S.mid_deg.begin() + (ptrdiff_t)mb));
         int64_t ooff = 0;
         for (int32_t v : big) {
             const int64_t deg = off[v + 1] - off[v];
@@ -689,6 +691,7 @@ PipeArgs Engine::pipe_args(const Scope &sc) const
     q.v1 = sc.v1;
     q.bsum = (int64_t *)b_bsum.p;
     q.last_v = sc.last_v;
+    q.narrow_cut = variant.cta_narrow ? sc.nnarrow : -1;
     return q;
 }
 
@@ -698,6 +701,16 @@ int Engine::launch_limits()
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_mid, count_mid64_kernel, 32 * kMidWarps, 0));
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_resolve, resolve_small_kernel, kTB, 0));
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_resolve_mid, resolve_mid_kernel, kTB, 0));
+    // the CTA kernels loop over their vertex range: a grid of exactly the resident blocks
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cta64, count_cta_kernel<64, 2 * kNarrowMax>, 64,
+                                                            sizeof(unsigned long long) * 2 * kNarrowMax));
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cta128, count_cta_kernel<128, 2 * kLargeAMax>, 128,
+                                                            sizeof(unsigned long long) * 2 * kLargeAMax));
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_cta256, count_cta_kernel<kTB, 2 * kLargeMax>, kTB,
+                                                            sizeof(unsigned long long) * 2 * kLargeMax));
+    occ_cta64 = std::max(occ_cta64, 1);
+    occ_cta128 = std::max(occ_cta128, 1);
+    occ_cta256 = std::max(occ_cta256, 1);
     occ_mid = std::max(occ_mid, 1);
     occ_resolve = std::max(occ_resolve, 1);
     occ_resolve_mid = std::max(occ_resolve_mid, 1);
@@ -759,8 +772,13 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
                                                     (int64_t)sms * std::min(mid_bps, occ_mid)),
                              32 * kMidWarps, 0, st>>>(q);
         launched("count_mid64_kernel", st);
-        const int g128 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * 10));
-        const int g256 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * 5));
+        const int g128 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * occ_cta128));
+        const int g256 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * occ_cta256));
+        if (q.narrow_cut > 0) {  // the lower part of the 128-thread range, in 64-thread CTAs
+            const int g64 = (int)std::min<int64_t>(q.narrow_cut, (int64_t)sms * occ_cta64);
+            count_cta_kernel<64, 2 * kNarrowMax><<<g64, 64, sizeof(unsigned long long) * 2 * kNarrowMax, st>>>(q, 4);
+            launched("count_cta_kernel<64>", st);
+        }
         if (variant.cta_stage) {  // neighbour IDs staged by bulk copies (the stage follows the table)
             count_cta_kernel<128, 2 * kLargeAMax, true>
                 <<<g128, 128, sizeof(unsigned long long) * 2 * kLargeAMax + sizeof(int32_t) * (kLargeAMax + 8), st>>>(
@@ -1298,7 +1316,7 @@ int galp_schedule_info(galp_ctx *ctx, galp_sched_info *info)
     info->nlarge = nml;
     info->nbig = (int64_t)E.sched.big_v.size();
     info->table_slots = E.sched.max_pair_slots;
-    info->launches_per_iter = 14 + (info->nbig ? 7 : 0) + (E.frontier ? 1 : 0);
+    info->launches_per_iter = 14 + (info->nbig ? 7 : 0) + (E.frontier ? 1 : 0) + (E.variant.cta_narrow ? 1 : 0);
     info->flags = (E.adj_sorted ? GALP_SCHED_SORTED : 0) | (E.symmetric ? GALP_SCHED_SYMMETRIC : 0) |
                   (E.frontier ? GALP_SCHED_FRONTIER : 0);
     info->launches = E.launches;
@@ -1310,7 +1328,7 @@ int galp_set_variant(galp_ctx *ctx, const galp_variant *v)
 {
     if (!ctx || !v || v->agg_mode < 0 || v->agg_mode > 2 || !(v->frontier_frac >= 0.f && v->frontier_frac <= 1.f) ||
         !(v->learned_margin >= 0.f && v->learned_margin < 10.f) || v->small_sort < 0 || v->small_sort > 2 ||
-        v->cta_stage < 0 || v->cta_stage > 1)
+        v->cta_stage < 0 || v->cta_stage > 1 || v->cta_narrow < 0 || v->cta_narrow > 1)
         return GALP_EINVAL;
     if (v->hub_part_shift < -16 || v->hub_part_shift > kMaxHubShift) return GALP_EINVAL;
     if (v->hub_part_shift != ctx->eng.sched.hub_shift) {

@@ -54,6 +54,7 @@ struct Scope {
     int32_t c0 = 0, nc = 0;    // big insert chunks
     int32_t s0 = 0, ns = 0;    // big stats chunks
     int32_t sv0 = 0, nsv = 0;  // vertices of degree <= 32 (small_v), in vertex order
+    int32_t nnarrow = 0;       // mid-list entries of at most kNarrowMax neighbours
     int32_t last_v = -1;       // last vertex of the scope that owns runs
     int32_t q0 = 0, nq = 0;    // hash partitions of the scope's big vertices
     int64_t pair_slots = 0;    // pair area of those partitions
@@ -216,7 +217,7 @@ struct Engine {
     bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
     bool symmetric = false;   // edge multiset symmetric (frontier marking along out-edges)
     Profiler prof;
-    galp_variant variant{0, 0.05f, 0.03f, 0, 0, 0, {}};  // kernel variant knobs (galp_set_variant)
+    galp_variant variant{0, 0.05f, 0.03f, 2, 0, 0, 1, 0};  // kernel variant knobs (galp_set_variant)
     // out-of-core streaming
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
@@ -240,6 +241,7 @@ struct Engine {
     // API): their grid-stride loops run as one full wave, since a partial second wave
     // would start its blocks' whole shares late
     int occ_mid = 0, occ_resolve = 0, occ_resolve_mid = 0;
+    int occ_cta64 = 0, occ_cta128 = 0, occ_cta256 = 0;  // resident CTA-kernel blocks per SM
     int launch_limits();
     // hub partitions at 2^shift times the default count: plan, upload, size the pair area
     int setup_hub_parts(int shift, cudaStream_t st, int64_t &h2d);

@@ -42,6 +42,8 @@ constexpr int kXlSlots = 2 * kXlMax; // 192 KB of shared-memory table (64-bit sl
 constexpr int kXlThreads = 1024;
 constexpr int kLargeAMax = 1024;     // large vertices up to here: 128-thread CTAs, 16 KB tables
 constexpr int kXlAMax = 6144;        // xl vertices up to here: 512-thread CTAs, 96 KB tables
+constexpr int kNarrowMax = 512;      // narrow CTA variant: large vertices up to here, 64 threads,
+                                     // 8 KB tables
 
 struct PipeArgs {
     const int32_t *nbr;     // neighbour buffer holding CSR entries [nbr_shift, ...)
@@ -88,6 +90,9 @@ struct PipeArgs {
     int32_t lab27;          // every label below 2^27 - 1 (32-bit sort keys in packs)
     int32_t small_sort;     // small vertices: 0 match-based packs, 1 sort-based packs (needs lab27),
                             // 2 one thread per vertex
+    int32_t narrow_cut;     // -1, or the mid-list position of the first vertex above kNarrowMax
+                            // neighbours: the 128-thread CTA range is split there, its lower
+                            // part going to 64-thread CTAs
 };
 
 // Graph of vertex v in batched mode: the largest g with g_v0[g] <= v.
@@ -541,22 +546,13 @@ __device__ __forceinline__ void t64_insert_row(unsigned long long *tab, uint32_t
     }
 }
 
-// Aggregate inserts when the vertex had at most half as many distinct labels as
-// neighbours in the previous iteration (agg_mode 0); always (1); never (2).
-__device__ __forceinline__ bool use_aggregation(const PipeArgs &p, int v, int deg)
-{
-    const int mode = p.disp->agg_mode;
-    return mode == 1 || (mode == 0 && 2 * p.dcnt[v] <= deg);
-}
-
 // Finish a counted vertex: per-vertex state, and its label unless it is tied.  One
 // thread; returns whether the vertex is tied (the caller appends it to the tied list).
 __device__ __forceinline__ bool finish_counted(const PipeArgs &p, int v, const Sum5 &s, int rmin, int rmax,
-                                               unsigned long long &changes)
+                                               unsigned long long &changes, int32_t old)
 {
     p.dcnt[v] = s.d;
     p.sm_kw[v] = s.k | (s.W << 16);
-    const int32_t old = __ldg(&p.lab_in[v]);
     if (s.k == 1) {
         p.lab_out[v] = s.mn;
         count_change(changes, s.mn, old);
@@ -567,6 +563,12 @@ __device__ __forceinline__ bool finish_counted(const PipeArgs &p, int v, const S
     p.sm_c1[v] = s.mx;
     p.sm_r[v] = rmin | (rmax << 16);
     return true;
+}
+
+__device__ __forceinline__ bool finish_counted(const PipeArgs &p, int v, const Sum5 &s, int rmin, int rmax,
+                                               unsigned long long &changes)
+{
+    return finish_counted(p, v, s, rmin, rmax, changes, __ldg(&p.lab_in[v]));
 }
 
 // Frontier: a clean vertex keeps its counts; it is re-resolved if tied, else keeps its
@@ -881,8 +883,39 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t pari
     return false;
 }
 
+// What a CTA needs of a mid-list vertex before counting it: loaded one vertex ahead, so
+// these dependent loads (list entry, then offsets and state) are in flight while the
+// previous vertex is counted.
+struct CtaHead {
+    int v;         // vertex, -1 past the end of the range
+    int deg;
+    int64_t o0;    // first CSR entry
+    int dcnt;      // distinct labels in the previous iteration (aggregation rule)
+    int32_t old;   // current label
+    int dirty;     // 0: frontier mode and no neighbour label changed
+};
+
+__device__ __forceinline__ CtaHead cta_head(const PipeArgs &p, int first, int i, int count, bool fr)
+{
+    CtaHead h{-1, 0, 0, 0, 0, 1};
+    if (i < count) {
+        h.v = p.mid_v[first + i];
+        h.o0 = __ldg(&p.off[h.v]);
+        h.deg = (int)(__ldg(&p.off[h.v + 1]) - h.o0);
+        h.dcnt = p.dcnt[h.v];
+        h.old = __ldg(&p.lab_in[h.v]);
+        h.dirty = fr ? (int)p.dirty[h.v] : 1;
+    }
+    return h;
+}
+
 // One CTA of THREADS threads per vertex of degree <= SLOTS/2 (table of SLOTS 64-bit
 // slots in dynamic shared memory), for a range of the degree-sorted mid list.
+//
+// Software pipelining across the CTA's vertices: the next vertex's head (CtaHead) and,
+// unless staged, its first PER * THREADS neighbour IDs are loaded into registers while
+// the current vertex's labels are gathered and counted, so a vertex starts with its
+// label gathers instead of three dependent global round trips.
 //
 // STAGE: the next vertex's neighbour IDs are copied into a shared-memory stage by one
 // bulk copy (cp.async.bulk, completion on an mbarrier) while the current vertex is
@@ -893,7 +926,8 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t pari
 // once more before the CTA exits and counts the remaining vertices from global loads.
 // Not in frontier mode (clean vertices need no IDs).
 template <int THREADS, int SLOTS, bool STAGE = false>
-__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 ? 2 : THREADS >= 256 ? 5 : 10)
+__global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 ? 2 : THREADS >= 256 ? 4
+                                           : THREADS >= 128 ? 8 : 16)
     count_cta_kernel(PipeArgs p, int which)
 {
     extern __shared__ __align__(16) unsigned long long cta_tab[];
@@ -906,10 +940,15 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     if (!ctl_active(p.ctl)) return;
     if (threadIdx.x == 0) ctn = 0;  // ordered before thread 0's own uses
     // ranges of the degree-sorted mid list: 0 [pos1, pos_a), 1 [pos_a, pos2), 2 [pos2, pos_b),
-    // 3 [pos_b, end)
+    // 3 [pos_b, end); with a narrow cut c, 0 is [max(pos1, c), pos_a) and 4 [pos1, min(pos_a, c))
     const DispatchState &ds = *p.disp;
-    const int first = which == 0 ? ds.pos1 : which == 1 ? ds.pos_a : which == 2 ? ds.pos2 : ds.pos_b;
-    const int end = which == 0 ? ds.pos_a : which == 1 ? ds.pos2 : which == 2 ? ds.pos_b : p.nmid_s + p.nmid_l + p.nmid_x;
+    int first = which == 0 ? ds.pos1 : which == 1 ? ds.pos_a : which == 2 ? ds.pos2 : which == 3 ? ds.pos_b : ds.pos1;
+    int end = which == 0 ? ds.pos_a : which == 1 ? ds.pos2 : which == 2 ? ds.pos_b : which == 3 ? p.nmid_s + p.nmid_l + p.nmid_x
+                                                                                            : ds.pos_a;
+    if (p.narrow_cut >= 0) {
+        if (which == 0) first = max(first, p.narrow_cut);
+        if (which == 4) end = min(end, p.narrow_cut);
+    }
     const int count = end - first;
     const bool fr = frontier_on(p);
     const int tid = threadIdx.x;
@@ -938,10 +977,31 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
         stage_issue(blockIdx.x);
     }
     __syncthreads();
+    constexpr int PER = 8;  // a thread's loads in flight together per round
+    // The first round of a vertex's neighbour IDs, loaded one vertex ahead (not staged; CTAs
+    // of up to 256 threads, whose vertices are short enough for the round trip to matter).
+    constexpr bool kAhead = THREADS <= 256;
+    const bool ahead = kAhead && !staged;
+    auto ids_ahead = [&](int (&nb)[PER], const CtaHead &h) {
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int e = tid + u * THREADS;
+            nb[u] = (ahead && h.v >= 0 && h.dirty && e < h.deg) ? ld_nbr(&p.nbr[h.o0 + e - p.nbr_shift]) : -1;
+        }
+    };
+    CtaHead nxt = cta_head(p, first, blockIdx.x, count, fr);
+    int nbn[PER];
+    ids_ahead(nbn, nxt);
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
-        const int v = p.mid_v[first + i];
-        if (fr && !p.dirty[v]) {
+        const CtaHead h = nxt;
+        const int v = h.v;
+        int nb0[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) nb0[u] = nbn[u];
+        nxt = cta_head(p, first, i + gridDim.x, count, fr);
+        if (!h.dirty) {
             if (tid == 0 && carry_clean(p, v)) tbuf_append(ctbuf, &ctn, v, p.tied_mid, &p.ctl->tied_mid);
+            ids_ahead(nbn, nxt);
             continue;
         }
         if (++gen > kT64GenMax) {
@@ -949,8 +1009,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
             __syncthreads();
             gen = 1;
         }
-        const int64_t o0 = __ldg(&p.off[v]);
-        const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
+        const int64_t o0 = h.o0;
+        const int deg = h.deg;
         // this vertex's IDs in the stage (the copy was issued one vertex earlier)
         bool from_stage = false;
         if (staged && stage_ok) {
@@ -968,16 +1028,20 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
         // probe range: the whole table up to 4 slots per neighbour (load <= 1/4 where the
         // table allows, at most 1/2): the longest probe of a warp's inserts sets its pace
         const uint32_t cap = (uint32_t)min(SLOTS, 4 * pad32(deg));
-        const bool agg = use_aggregation(p, v, deg);
+        // warp-aggregated inserts when the vertex had at most half as many distinct labels
+        // as neighbours in the previous iteration (agg_mode 0); always (1); never (2)
+        const int mode = p.disp->agg_mode;
+        const bool agg = mode == 1 || (mode == 0 && 2 * h.dcnt <= deg);
         Sum5 obs = sum5_empty();
-        // gather in rounds of PER loads per thread in flight together
-        constexpr int PER = 8;
+        // gather in rounds of PER loads per thread in flight together; the first round's IDs
+        // are in registers already (or in the stage)
         for (int base = 0; base < deg; base += THREADS * PER) {
             int nb[PER];
 #pragma unroll
             for (int u = 0; u < PER; ++u) {
                 const int e = base + tid + u * THREADS;
-                nb[u] = (e < deg) ? (from_stage ? stage[skip + e] : ld_nbr(&p.nbr[o0 + e - p.nbr_shift])) : -1;
+                if (base == 0 && ahead) nb[u] = nb0[u];
+                else nb[u] = (e < deg) ? (from_stage ? stage[skip + e] : ld_nbr(&p.nbr[o0 + e - p.nbr_shift])) : -1;
             }
             uint32_t lb[PER];
 #pragma unroll
@@ -988,6 +1052,9 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
                 t64_insert_row(cta_tab, cap, gen, lb[u], agg, obs);
             }
         }
+        // the next vertex's first IDs (its head has arrived during the gathers and inserts)
+        // load while this vertex is reduced, ranked, spilled and finished
+        ids_ahead(nbn, nxt);
         // the reduction's barrier also completes the table for the rank and spill passes,
         // and every thread's reads of the stage: the next vertex's copy may start
         const Sum5 s = br.reduce(obs);
@@ -1005,7 +1072,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
                           p.run_cnt + (o0 - p.nbr_shift), &sctr);
             }
         }
-        if (tid == 0 && finish_counted(p, v, s, rmin, rmax, changes))
+        if (tid == 0 && finish_counted(p, v, s, rmin, rmax, changes, h.old))
             tbuf_append(ctbuf, &ctn, v, p.tied_mid, &p.ctl->tied_mid);
         __syncthreads();
     }

@@ -60,14 +60,19 @@ typedef struct {
                               of labels changed recounts every vertex (default 0.05) */
     float learned_margin;  /* learned rule: predicted log gain needed to leave the fixed rule's
                               choice (default 0.03) */
-    int32_t small_sort;    /* packs of small vertices: 1 = sort-based counting, 0 = match-based */
+    int32_t small_sort;    /* vertices of at most 32 neighbours: 2 = one thread per vertex, labels sorted
+                              in shared memory (default); 1 = packs of vertices per warp, sort-based
+                              counting; 0 = packs per warp, match-based counting */
     int32_t hub_part_shift; /* hubs (above 12288 neighbours) count their labels in degree * 2^shift / 8192
                                hash partitions (default 0); a partition that overflows makes the run
                                redo itself with the shift raised by one (up to 6) */
     int32_t cta_stage;      /* CTA counting of 257..2048 neighbours: 1 = the next vertex's neighbour IDs
                                staged in shared memory by a bulk copy, 0 = global loads (default: the
                                stage takes unified L1 from the label gathers; 1.7x slower on R-MAT 26) */
-    int32_t pad[2];
+    int32_t cta_narrow;     /* 1 = vertices of 257..512 neighbours counted by 64-thread CTAs with 8 KB
+                               tables, split off the 128-thread CTA range (default); 0 = all of that
+                               range in 128-thread CTAs */
+    int32_t pad;
 } galp_variant;
 
 /* One row of the in-core variant table (every row computes the same labels). */

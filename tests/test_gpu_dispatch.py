@@ -66,11 +66,15 @@ def test_variant_table():
         assert r["frontier"] == (k & 1) and r["agg_mode"] == (1 if k & 8 else 2)
 
 
+@pytest.mark.parametrize("narrow", [0, 1])
 @pytest.mark.parametrize("row", range(16))
-def test_every_variant_row_is_exact(row):
+def test_every_variant_row_is_exact(row, narrow):
+    # every row's split of the degree-sorted mid list, with and without the 64-thread CTA
+    # range cut out of the 128-thread one (455 vertices of 257..512 neighbours)
     g = galp_gb300.generate_rmat(15, 16, seed=11)
     with galp_gb300.Propagator(g, frontier=1) as p:
         tools.dispatch_set(p, 2, row)
+        tools.set_variant(p, cta_narrow=narrow)
         p.run(8)
         got, its, upd = p.get_labels(), p.iters_run, list(p.updates)
         _, rows = tools.dispatch_log(p)

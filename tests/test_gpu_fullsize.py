@@ -72,20 +72,44 @@ def test_lfr_1m_ten_iterations_equal_the_oracle():
         assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("narrow", [0, 1])
 @pytest.mark.parametrize("stage", [0, 1])
-def test_cta_staging_on_and_off_equal_the_oracle(stage):
-    # CTA counting with the next vertex's neighbour IDs staged by bulk copies (default) or
-    # read from global memory: the same labels, in-core and out of core
+def test_cta_staging_on_and_off_equal_the_oracle(stage, narrow):
+    # CTA counting with the next vertex's neighbour IDs staged by bulk copies or read from
+    # global memory, with and without the 64-thread range: the same labels, in-core and
+    # out of core
     from galp_gb300 import tools
 
     g = galp_gb300.generate_rmat(17, 24, seed=11)
     assert ((g.degrees() > 256) & (g.degrees() <= 2048)).sum() > 100
     for opts in ({}, {"policy": 2, "buffer_pow": 18}):
         with galp_gb300.Propagator(g, early_exit=0, **opts) as p:
-            tools.set_variant(p, cta_stage=stage)
+            tools.set_variant(p, cta_stage=stage, cta_narrow=narrow)
             want = np.arange(g.n, dtype=np.int32)
             for k in range(1, 5):
                 want, _ = oracle.step_par(g.offsets, g.neighbors, want, policy=opts.get("policy", 0),
                                           buffer_pow=opts.get("buffer_pow", 24))
                 p.run(k)
                 assert np.array_equal(p.get_labels(), want), f"{opts} iteration {k}"
+
+
+@pytest.mark.parametrize("narrow", [0, 1])
+def test_narrow_cta_split_equals_the_oracle(narrow):
+    # vertices of 257..512 neighbours in 64-thread CTAs (8 KB tables) or in the 128-thread
+    # ones: the same labels, in-core with and without the frontier, and out of core
+    from galp_gb300 import tools
+
+    g = galp_gb300.generate_rmat(16, 24, seed=11)
+    assert ((g.degrees() > 256) & (g.degrees() <= 512)).sum() > 1000
+    for opts in ({}, {"frontier": 1}, {"policy": 2, "buffer_pow": 18}):
+        with galp_gb300.Propagator(g, early_exit=0, **opts) as p:
+            tools.set_variant(p, cta_narrow=narrow)
+            want = np.arange(g.n, dtype=np.int32)
+            counts = []
+            for k in range(1, 6):
+                want, c = oracle.step_par(g.offsets, g.neighbors, want, policy=opts.get("policy", 0),
+                                          buffer_pow=opts.get("buffer_pow", 24))
+                counts.append(c)
+                p.run(k)
+                assert np.array_equal(p.get_labels(), want), f"{opts} iteration {k}"
+                assert list(p.updates) == counts
