@@ -427,7 +427,9 @@ __device__ __forceinline__ uint32_t t64_insert(unsigned long long *tab, uint32_t
 {
     const unsigned long long tag = t64_tag(gen, label);
     uint32_t h = hslot(label, cap);
-    unsigned long long cur = *(volatile unsigned long long *)&tab[h];
+    // Plain loads: a slot that holds this vertex's generation never changes its label, and
+    // a stale view of a free slot is caught by the compare-and-swap.
+    unsigned long long cur = tab[h];
     for (;;) {
         if ((cur & ~kT64CntMask) == tag) {
             // the count is the low 14 bits of the low word (little-endian), and the total
@@ -445,7 +447,7 @@ __device__ __forceinline__ uint32_t t64_insert(unsigned long long *tab, uint32_t
             continue;
         }
         h = (h + 1 == cap) ? 0 : h + 1;
-        cur = *(volatile unsigned long long *)&tab[h];
+        cur = tab[h];
     }
 }
 
@@ -621,16 +623,37 @@ __global__ void __launch_bounds__(128, kSmallLaneBlocks) count_small_lane_kernel
     unsigned long long changes = 0;
     const int stride = gridDim.x * 128;
     // warp-uniform trip count: every lane runs the loop the same number of times
+    // a lane's next vertex: index, offsets, label and dirty flag load one round ahead
+    struct Head {
+        int v, deg;
+        int64_t o0;
+        int32_t old;
+        int dirty;
+    };
+    auto head = [&](int i) {
+        Head h{0, 0, 0, 0, 1};
+        if (i < p.nsmall) {
+            h.v = p.small_v[i];
+            h.o0 = __ldg(&p.off[h.v]);
+            h.deg = (int)(__ldg(&p.off[h.v + 1]) - h.o0);
+            h.old = __ldg(&p.lab_in[h.v]);
+            h.dirty = fr ? (int)p.dirty[h.v] : 1;
+        }
+        return h;
+    };
+    Head nxt = head(blockIdx.x * 128 + w * 32 + lane);
     for (int base = blockIdx.x * 128 + w * 32; base < p.nsmall; base += stride) {
         const int i = base + lane;
         const bool active = i < p.nsmall;
-        const int v = active ? p.small_v[i] : 0;
+        const Head h = nxt;
+        nxt = head(i + stride);
+        const int v = h.v;
         bool tied = false, chg = false;
         if (active) {
-            const int64_t o0 = __ldg(&p.off[v]);
-            const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
-            const int32_t old = __ldg(&p.lab_in[v]);
-            if (fr && !p.dirty[v]) {
+            const int64_t o0 = h.o0;
+            const int deg = h.deg;
+            const int32_t old = h.old;
+            if (!h.dirty) {
                 // no label around the vertex changed: its counts carry over
                 tied = deg > 0 && (p.sm_kw[v] & 0xFFFF) > 1;
                 if (!tied) p.lab_out[v] = old;
@@ -715,6 +738,32 @@ __global__ void __launch_bounds__(128, kSmallLaneBlocks) count_small_lane_kernel
     flush_changes(changes, p.ctl);
 }
 
+// What a warp or CTA needs of a mid-list vertex before counting it: loaded one vertex ahead, so
+// these dependent loads (list entry, then offsets and state) are in flight while the
+// previous vertex is counted.
+struct CtaHead {
+    int v;         // vertex, -1 past the end of the range
+    int deg;
+    int64_t o0;    // first CSR entry
+    int dcnt;      // distinct labels in the previous iteration (aggregation rule)
+    int32_t old;   // current label
+    int dirty;     // 0: frontier mode and no neighbour label changed
+};
+
+__device__ __forceinline__ CtaHead cta_head(const PipeArgs &p, int first, int i, int count, bool fr)
+{
+    CtaHead h{-1, 0, 0, 0, 0, 1};
+    if (i < count) {
+        h.v = p.mid_v[first + i];
+        h.o0 = __ldg(&p.off[h.v]);
+        h.deg = (int)(__ldg(&p.off[h.v + 1]) - h.o0);
+        h.dcnt = p.dcnt[h.v];
+        h.old = __ldg(&p.lab_in[h.v]);
+        h.dirty = fr ? (int)p.dirty[h.v] : 1;
+    }
+    return h;
+}
+
 // One warp per mid vertex (33..256 neighbours): a 512-slot table of generation-tagged
 // 64-bit slots per warp (as the CTA tables: never cleared between vertices), probed over
 // up to 4 slots per neighbour.  Against 32-bit key and count arrays cleared per vertex:
@@ -735,10 +784,28 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
     uint32_t gen = 0;
     __syncwarp();
     const int nwarp_v = p.disp->pos1;  // the degree-sorted mid list's prefix of warp vertices
+    constexpr int PER = kMidSMax / 32;
+    // the next vertex's head and neighbour IDs load while the current one is counted
+    auto ids_ahead = [&](int (&nb)[PER], const CtaHead &h) {
+#pragma unroll
+        for (int u = 0; u < PER; ++u) {
+            const int e = lane + u * 32;
+            nb[u] = (h.v >= 0 && h.dirty && e < h.deg) ? ld_nbr(&p.nbr[h.o0 + e - p.nbr_shift]) : -1;
+        }
+    };
+    CtaHead nxt = cta_head(p, 0, gw, nwarp_v, fr);
+    int nbn[PER];
+    ids_ahead(nbn, nxt);
     for (int i = gw; i < nwarp_v; i += nw) {
-        const int v = p.mid_v[i];
-        if (fr && !p.dirty[v]) {
+        const CtaHead h = nxt;
+        const int v = h.v;
+        int nb[PER];
+#pragma unroll
+        for (int u = 0; u < PER; ++u) nb[u] = nbn[u];
+        nxt = cta_head(p, 0, i + nw, nwarp_v, fr);
+        if (!h.dirty) {
             tb.append(lane == 0 && carry_clean(p, v), v, p.tied_mid, &p.ctl->tied_mid);
+            ids_ahead(nbn, nxt);
             continue;
         }
         if (++gen > kT64GenMax) {
@@ -746,16 +813,9 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
             __syncwarp();
             gen = 1;
         }
-        const int64_t o0 = __ldg(&p.off[v]);
-        const int deg = (int)(__ldg(&p.off[v + 1]) - o0);
+        const int64_t o0 = h.o0;
+        const int deg = h.deg;
         const uint32_t cap = (uint32_t)min(kMidSCap, 4 * pad32(deg));
-        constexpr int PER = kMidSMax / 32;
-        int nb[PER];
-#pragma unroll
-        for (int u = 0; u < PER; ++u) {
-            const int e = lane + u * 32;
-            nb[u] = (e < deg) ? ld_nbr(&p.nbr[o0 + e - p.nbr_shift]) : -1;
-        }
         uint32_t lb[PER];
 #pragma unroll
         for (int u = 0; u < PER; ++u) lb[u] = (nb[u] >= 0) ? (uint32_t)ld_label(&p.lab_in[nb[u]]) : kEmpty;
@@ -766,6 +826,7 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
             // lanes holding the same label add once (heavy labels would serialise)
             t64_insert_row(tab, cap, gen, lb[u], true, part);
         }
+        ids_ahead(nbn, nxt);
         __syncwarp();
         const Sum5 sm = sum5_warp(part);
         int rmin = 0, rmax = sm.d - 1;  // when every distinct label is a candidate
@@ -792,7 +853,7 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
                 }
             }
         }
-        const bool tied = lane == 0 && finish_counted(p, v, sm, rmin, rmax, changes);
+        const bool tied = lane == 0 && finish_counted(p, v, sm, rmin, rmax, changes, h.old);
         tb.append(tied, v, p.tied_mid, &p.ctl->tied_mid);
         __syncwarp();
     }
@@ -800,28 +861,29 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
     flush_changes(changes, p.ctl);
 }
 
-// Block-wide Sum5 / pair reductions through shared memory (two barriers each).
-// Block-wide reductions with one barrier each: warps publish partials, then every warp
-// folds all of them.  Sum5 and the rank pair use separate buffers, and the kernel's
-// end-of-vertex barrier orders a buffer's reads before its next writes.
+// Block-wide Sum5 / pair reductions with one barrier each: warps publish partials, then
+// every warp folds all of them.  Buffers hold one entry per warp (W = THREADS / 32): buf
+// is [5][W], buf2 [2][W].  The kernel's end-of-vertex barrier orders a buffer's reads
+// before its next writes.
 template <int THREADS>
 struct BlockRed5 {
-    int (*buf)[32];   // [5][32]
-    int (*buf2)[32];  // [2][32]
+    static constexpr int W = THREADS / 32;
+    int *buf;   // [5][W]
+    int *buf2;  // [2][W]
     __device__ Sum5 reduce(Sum5 s) const
     {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         s = sum5_warp(s);
         if (lane == 0) {
-            buf[0][warp] = s.d;
-            buf[1][warp] = s.W;
-            buf[2][warp] = s.k;
-            buf[3][warp] = s.mn;
-            buf[4][warp] = s.mx;
+            buf[0 * W + warp] = s.d;
+            buf[1 * W + warp] = s.W;
+            buf[2 * W + warp] = s.k;
+            buf[3 * W + warp] = s.mn;
+            buf[4 * W + warp] = s.mx;
         }
         __syncthreads();
         Sum5 t = sum5_empty();
-        if (lane < THREADS / 32) t = Sum5{buf[0][lane], buf[1][lane], buf[2][lane], buf[3][lane], buf[4][lane]};
+        if (lane < W) t = Sum5{buf[lane], buf[W + lane], buf[2 * W + lane], buf[3 * W + lane], buf[4 * W + lane]};
         return sum5_warp(t);
     }
     __device__ void reduce2(int &a, int &b) const
@@ -830,11 +892,11 @@ struct BlockRed5 {
         a = __reduce_add_sync(kFull, a);
         b = __reduce_add_sync(kFull, b);
         if (lane == 0) {
-            buf2[0][warp] = a;
-            buf2[1][warp] = b;
+            buf2[warp] = a;
+            buf2[W + warp] = b;
         }
         __syncthreads();
-        const int x = lane < THREADS / 32 ? buf2[0][lane] : 0, y = lane < THREADS / 32 ? buf2[1][lane] : 0;
+        const int x = lane < W ? buf2[lane] : 0, y = lane < W ? buf2[W + lane] : 0;
         a = __reduce_add_sync(kFull, x);
         b = __reduce_add_sync(kFull, y);
     }
@@ -883,32 +945,6 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t pari
     return false;
 }
 
-// What a CTA needs of a mid-list vertex before counting it: loaded one vertex ahead, so
-// these dependent loads (list entry, then offsets and state) are in flight while the
-// previous vertex is counted.
-struct CtaHead {
-    int v;         // vertex, -1 past the end of the range
-    int deg;
-    int64_t o0;    // first CSR entry
-    int dcnt;      // distinct labels in the previous iteration (aggregation rule)
-    int32_t old;   // current label
-    int dirty;     // 0: frontier mode and no neighbour label changed
-};
-
-__device__ __forceinline__ CtaHead cta_head(const PipeArgs &p, int first, int i, int count, bool fr)
-{
-    CtaHead h{-1, 0, 0, 0, 0, 1};
-    if (i < count) {
-        h.v = p.mid_v[first + i];
-        h.o0 = __ldg(&p.off[h.v]);
-        h.deg = (int)(__ldg(&p.off[h.v + 1]) - h.o0);
-        h.dcnt = p.dcnt[h.v];
-        h.old = __ldg(&p.lab_in[h.v]);
-        h.dirty = fr ? (int)p.dirty[h.v] : 1;
-    }
-    return h;
-}
-
 // One CTA of THREADS threads per vertex of degree <= SLOTS/2 (table of SLOTS 64-bit
 // slots in dynamic shared memory), for a range of the degree-sorted mid list.
 //
@@ -931,7 +967,7 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     count_cta_kernel(PipeArgs p, int which)
 {
     extern __shared__ __align__(16) unsigned long long cta_tab[];
-    __shared__ int red[5][32], red2[2][32];
+    __shared__ int red[5 * (THREADS / 32)], red2[2 * (THREADS / 32)];
     __shared__ int sctr;
     __shared__ __align__(8) unsigned long long stage_bar;
     __shared__ int stage_ok;
@@ -979,7 +1015,8 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
     __syncthreads();
     constexpr int PER = 8;  // a thread's loads in flight together per round
     // The first round of a vertex's neighbour IDs, loaded one vertex ahead (not staged; CTAs
-    // of up to 256 threads, whose vertices are short enough for the round trip to matter).
+    // of up to 256 threads: in the 512- and 1024-thread CTAs the extra registers cost the
+    // gathers more than the early IDs save).
     constexpr bool kAhead = THREADS <= 256;
     const bool ahead = kAhead && !staged;
     auto ids_ahead = [&](int (&nb)[PER], const CtaHead &h) {
@@ -1092,7 +1129,7 @@ __global__ void __launch_bounds__(kHubCountThreads, 1) hub_count_kernel(IterArgs
 {
     constexpr int kT = kHubCountThreads;
     extern __shared__ __align__(16) uint32_t hub_tab[];  // kHubTab keys, then kHubTab counts
-    __shared__ int red[5][32], red2[2][32];
+    __shared__ int red[5 * (kHubCountThreads / 32)], red2[2 * (kHubCountThreads / 32)];
     __shared__ int sfill, sbase, sctr;
     if (!ctl_active(p.ctl)) return;
     uint32_t *key = hub_tab;
