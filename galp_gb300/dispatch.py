@@ -41,7 +41,8 @@ def training_graphs(seed: int = 7):
     specs = []
     rmats = [(16, 8, 0.57), (17, 16, 0.57), (18, 16, 0.57), (18, 32, 0.45), (19, 8, 0.45), (19, 16, 0.57),
              (20, 16, 0.57), (20, 8, 0.50), (21, 4, 0.57), (17, 32, 0.65), (18, 8, 0.65), (19, 32, 0.50),
-             (20, 32, 0.57), (21, 16, 0.57), (21, 8, 0.45), (22, 8, 0.57), (22, 16, 0.50), (16, 64, 0.57)]
+             (20, 32, 0.57), (21, 16, 0.57), (21, 8, 0.45), (22, 8, 0.57), (22, 16, 0.50), (16, 64, 0.57),
+             (23, 16, 0.57), (24, 16, 0.57)]
     for scale, ef, a in rmats:
         b = c = (1 - a) / 3 if a < 0.57 else (1 - a) / 2.27
         specs.append((f"rmat{scale}-ef{ef}-a{a}", lambda s=scale, e=ef, a=a, b=b, c=c: generate_rmat(s, e, a, b, c,
