@@ -409,7 +409,7 @@ int Engine::setup(const galp_csr &g, const galp_opts &o, cudaStream_t st, int64_
     if ((rc = upload(b_schunk_big, d_schunk_big, sched.schunk_big, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s0, d_schunk_s0, sched.schunk_s0, st, h2d))) return rc;
     if ((rc = upload(b_schunk_s1, d_schunk_s1, sched.schunk_s1, st, h2d))) return rc;
-    if ((rc = setup_hub_parts(0, st, h2d))) return rc;
+    if ((rc = setup_hub_parts(variant.hub_part_shift, st, h2d))) return rc;
     // per-vertex state, spill and tied lists
     const size_t nn = (size_t)std::max<int64_t>(n, 1);
     GALP_CUDA(b_dcnt.alloc(sizeof(int32_t) * nn));
@@ -564,11 +564,20 @@ int Engine::setup_hub_parts(int shift, cudaStream_t st, int64_t &h2d)
     GALP_CUDA(b_psum.alloc(sizeof(int4) * nparts));
     GALP_CUDA(b_pairs.alloc(sizeof(unsigned long long) * (size_t)std::max<int64_t>(sched.max_pair_slots, 1)));
     if (!hub_count_blocks && !sched.part_big.empty()) {
-        const int smem = (int)(sizeof(uint32_t) * 2 * kHubTab);
-        GALP_CUDA(cudaFuncSetAttribute(hub_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        int occ = 0;
-        GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, hub_count_kernel, kHubCountThreads, smem));
+        const int smem = (int)(sizeof(uint32_t) * 2 * kHubTab), smem2 = (int)(sizeof(uint32_t) * kHubTab),
+                  smem4 = (int)(sizeof(uint32_t) * kHubTab / 2);
+        auto *k1 = hub_count_kernel<kHubCountThreads, kHubTab>;
+        auto *k2 = hub_count_kernel<kHubCountThreads / 2, kHubTab / 2>;
+        auto *k4 = hub_count_kernel<kHubCountThreads / 4, kHubTab / 4>;
+        GALP_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        GALP_CUDA(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, smem2));
+        int occ = 0, occ2 = 0, occ4 = 0;
+        GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k1, kHubCountThreads, smem));
+        GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, k2, kHubCountThreads / 2, smem2));
+        GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ4, k4, kHubCountThreads / 4, smem4));
         hub_count_blocks = std::max(occ, 1) * sms;
+        hub_count_blocks_half = std::max(occ2, 1) * sms;
+        hub_count_blocks_quarter = std::max(occ4, 1) * sms;
     }
     GALP_CUDA(cudaStreamSynchronize(st));
     return GALP_OK;
@@ -743,8 +752,18 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
         if (prof.on) e0 = prof.mark(st);
         big_insert_kernel<<<a.nchunks, kTB, 0, st>>>(a);
         launched("big_insert_kernel", st);
-        hub_count_kernel<<<std::min(a.nparts, hub_count_blocks), kHubCountThreads, sizeof(uint32_t) * 2 * kHubTab,
-                           st>>>(a);
+        // smaller partitions (hub_part_shift), smaller tables and more CTAs per SM
+        if (sched.hub_shift >= 2)
+            hub_count_kernel<kHubCountThreads / 4, kHubTab / 4>
+                <<<std::min(a.nparts, hub_count_blocks_quarter), kHubCountThreads / 4,
+                   sizeof(uint32_t) * kHubTab / 2, st>>>(a);
+        else if (sched.hub_shift == 1)
+            hub_count_kernel<kHubCountThreads / 2, kHubTab / 2>
+                <<<std::min(a.nparts, hub_count_blocks_half), kHubCountThreads / 2, sizeof(uint32_t) * kHubTab,
+                   st>>>(a);
+        else
+            hub_count_kernel<kHubCountThreads, kHubTab>
+                <<<std::min(a.nparts, hub_count_blocks), kHubCountThreads, sizeof(uint32_t) * 2 * kHubTab, st>>>(a);
         launched("hub_count_kernel", st);
         big_combine_kernel<<<(a.nbig + 7) / 8, 256, 0, st>>>(a);
         launched("big_combine_kernel", st);

@@ -217,7 +217,7 @@ struct Engine {
     bool adj_sorted = false;  // every adjacency list strictly increasing (first-iteration shortcut)
     bool symmetric = false;   // edge multiset symmetric (frontier marking along out-edges)
     Profiler prof;
-    galp_variant variant{0, 0.05f, 0.03f, 2, 0, 0, 1, 0};  // kernel variant knobs (galp_set_variant)
+    galp_variant variant{0, 0.05f, 0.03f, 2, 1, 0, 1, 0};  // kernel variant knobs (galp_set_variant)
     // out-of-core streaming
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_consumed[2] = {nullptr, nullptr};
@@ -225,6 +225,7 @@ struct Engine {
     int64_t h2d_run = 0;      // bytes streamed by the last run
     int64_t launches = 0;     // kernels launched by runs so far (setup excluded)
     int hub_count_blocks = 0; // resident blocks of hub_count_kernel (grid = one wave)
+    int hub_count_blocks_half = 0, hub_count_blocks_quarter = 0;  // the same for its smaller shapes
     double setup_ms[5] = {};  // host schedule, CSR upload, state upload, dispatch prep, device checks
     // batched mode: graph g = vertices [g_v0[g], g_v0[g+1]) of the concatenated CSR
     bool batched = false;

@@ -1125,15 +1125,19 @@ __global__ void __launch_bounds__(THREADS, THREADS >= 1024 ? 1 : THREADS >= 512 
 // label fall in one partition, so its count is complete here), fold the counts each
 // insert observes into the partition's summary, append its distinct labels to the hub's
 // distinct list and reset the partition's fill for the next scope.
-__global__ void __launch_bounds__(kHubCountThreads, 1) hub_count_kernel(IterArgs p)
+//
+// Three shapes: 1024 threads with 16384-slot tables (one CTA per SM), 512 threads with
+// 8192-slot tables (three per SM) for partitions of half the size (hub_part_shift 1), and
+// 256 threads with 4096-slot tables (six per SM) for a quarter (hub_part_shift >= 2).
+template <int kT, int TAB>
+__global__ void __launch_bounds__(kT, kT >= 1024 ? 1 : kT >= 512 ? 3 : 6) hub_count_kernel(IterArgs p)
 {
-    constexpr int kT = kHubCountThreads;
-    extern __shared__ __align__(16) uint32_t hub_tab[];  // kHubTab keys, then kHubTab counts
-    __shared__ int red[5 * (kHubCountThreads / 32)], red2[2 * (kHubCountThreads / 32)];
+    extern __shared__ __align__(16) uint32_t hub_tab[];  // TAB keys, then TAB counts
+    __shared__ int red[5 * (kT / 32)], red2[2 * (kT / 32)];
     __shared__ int sfill, sbase, sctr;
     if (!ctl_active(p.ctl)) return;
     uint32_t *key = hub_tab;
-    uint32_t *cnt = hub_tab + kHubTab;
+    uint32_t *cnt = hub_tab + TAB;
     const BlockRed5<kT> br{red, red2};
     const int tid = threadIdx.x, lane = tid & 31;
     for (int x = blockIdx.x; x < p.nparts; x += gridDim.x) {
@@ -1144,7 +1148,7 @@ __global__ void __launch_bounds__(kHubCountThreads, 1) hub_count_kernel(IterArgs
         __syncthreads();
         const int fill = sfill;
         uint32_t tcap = 64;  // load <= 1/2 when every pair is a distinct label
-        while (tcap < 2u * (uint32_t)fill && tcap < (uint32_t)kHubTab) tcap <<= 1;
+        while (tcap < 2u * (uint32_t)fill && tcap < (uint32_t)TAB) tcap <<= 1;
         for (int s2 = tid; s2 < (int)tcap; s2 += kT) {
             key[s2] = kEmpty;
             cnt[s2] = 0;

@@ -64,8 +64,10 @@ typedef struct {
                               in shared memory (default); 1 = packs of vertices per warp, sort-based
                               counting; 0 = packs per warp, match-based counting */
     int32_t hub_part_shift; /* hubs (above 12288 neighbours) count their labels in degree * 2^shift / 8192
-                               hash partitions (default 0); a partition that overflows makes the run
-                               redo itself with the shift raised by one (up to 6) */
+                               hash partitions (default 1); a partition that overflows makes the run
+                               redo itself with the shift raised by one (up to 6).  Shift 0 counts a
+                               partition in a 1024-thread CTA with a 128 KB table, 1 in 512 threads
+                               with 64 KB (three per SM), 2 and above in 256 threads with 32 KB (six) */
     int32_t cta_stage;      /* CTA counting of 257..2048 neighbours: 1 = the next vertex's neighbour IDs
                                staged in shared memory by a bulk copy, 0 = global loads (default: the
                                stage takes unified L1 from the label gathers; 1.7x slower on R-MAT 26) */

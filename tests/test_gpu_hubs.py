@@ -115,13 +115,14 @@ def test_hubs_inside_out_of_core_batches(hub_graph, policy, bpow):
                 break
 
 
-@pytest.mark.parametrize("shift", [-6, 2])
+@pytest.mark.parametrize("shift", [-6, 0, 2])
 def test_hub_partition_count_does_not_change_labels(hub_graph, shift):
     """Hubs count their labels in degree * 2^shift / 8192 hash partitions.
     With far too few partitions (shift -6: one per hub, whose table holds fewer distinct
     labels than the hub's neighbours carry) the first iterations overflow them; the run is
-    redone with twice the partitions until none overflows, and its labels are exact.  More
-    partitions (shift 2) are exact too."""
+    redone with twice the partitions until none overflows, and its labels are exact.  The
+    other partition sizes, each counted by its own CTA shape (shift 0: 1024 threads, the
+    default 1: 512, 2: 256), are exact too."""
     with galp_gb300.Propagator(hub_graph) as p:
         tools.set_variant(p, hub_part_shift=shift)
         for k in (1, 2, 3, 10):
