@@ -11,7 +11,7 @@
 //   * learned: a 3-layer MLP (kFeat -> kHid -> kHid -> kVar, ReLU, FP32) predicts the
 //     log slowdown of every variant from the iteration's features; the argmin wins when
 //     it is predicted to beat the fixed rule's row by more than a margin (the fixed rule
-//     is the fallback and the judge);
+//     is the fallback and the reference point);
 //   * forced: one variant for every iteration (timing sweeps that train the MLP).
 // The features of every iteration are logged for those sweeps.
 #pragma once
