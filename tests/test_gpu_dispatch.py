@@ -107,6 +107,23 @@ def test_dispatch_set_validates():
             tools.dispatch_set(p, 1, 0, np.zeros(5, np.float32))
 
 
+def test_variant_defaults_and_validation():
+    # the defaults this build measures with, and out-of-range knobs rejected without
+    # changing the variant in force
+    g = galp_gb300.generate_sbm([64] * 8, 8.0, 1.0, seed=1)
+    with galp_gb300.Propagator(g) as p:
+        v = tools.set_variant(p)
+        assert (v.small_sort, v.cta_narrow, v.cta_stage, v.agg_mode, v.hub_part_shift) == (2, 1, 0, 0, 1)
+        for bad in ({"small_sort": 3}, {"small_sort": -1}, {"cta_narrow": 2}, {"cta_stage": 2},
+                    {"agg_mode": 3}, {"frontier_frac": 1.5}, {"hub_part_shift": 99}):
+            with pytest.raises(RuntimeError):
+                tools.set_variant(p, **bad)
+        assert tools.set_variant(p).small_sort == 2
+        p.run(5)
+        it, want, counts = oracle.run(g.offsets, g.neighbors, 5)
+        assert p.iters_run == it and np.array_equal(p.get_labels(), want)
+
+
 def test_builtin_learned_dispatch_is_exact_and_not_slower():
     """opts.dispatch = 1 loads the network trained on this machine's timing sweeps; it
     changes only speed, and must not make a run slower than the fixed rule (2 % allowance
