@@ -708,6 +708,8 @@ PipeArgs Engine::pipe_args(const Scope &sc) const
 int Engine::launch_limits()
 {
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_mid, count_mid64_kernel, 32 * kMidWarps, 0));
+    GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_mid_sort, count_mid_sort_kernel, 32 * kMidWarps, 0));
+    occ_mid_sort = std::max(occ_mid_sort, 1);
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_resolve, resolve_small_kernel, kTB, 0));
     GALP_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_resolve_mid, resolve_mid_kernel, kTB, 0));
     // the CTA kernels loop over their vertex range: a grid of exactly the resident blocks
@@ -787,10 +789,15 @@ int Engine::enqueue_scope(cudaStream_t st, const Scope &sc, const int32_t *nbr, 
     }
     if (q.nmid_s + q.nmid_l + q.nmid_x) {
         // ranges of the degree-sorted mid list come from the dispatch state
-        count_mid64_kernel<<<(int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1,
-                                                    (int64_t)sms * std::min(mid_bps, occ_mid)),
-                             32 * kMidWarps, 0, st>>>(q);
-        launched("count_mid64_kernel", st);
+        const int gmid = (int)std::min<int64_t>((sc.nms + kMidWarps - 1) / kMidWarps + 1,
+                                                (int64_t)sms * std::min(mid_bps, variant.mid_sort ? occ_mid_sort : occ_mid));
+        if (variant.mid_sort) {  // sort + reduce counting of the warp range
+            count_mid_sort_kernel<<<gmid, 32 * kMidWarps, 0, st>>>(q);
+            launched("count_mid_sort_kernel", st);
+        } else {
+            count_mid64_kernel<<<gmid, 32 * kMidWarps, 0, st>>>(q);
+            launched("count_mid64_kernel", st);
+        }
         const int g128 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nms + sc.nml, (int64_t)sms * occ_cta128));
         const int g256 = (int)std::max<int64_t>(1, std::min<int64_t>(sc.nml, (int64_t)sms * occ_cta256));
         if (q.narrow_cut > 0) {  // the lower part of the 128-thread range, in 64-thread CTAs
@@ -1347,7 +1354,8 @@ int galp_set_variant(galp_ctx *ctx, const galp_variant *v)
 {
     if (!ctx || !v || v->agg_mode < 0 || v->agg_mode > 2 || !(v->frontier_frac >= 0.f && v->frontier_frac <= 1.f) ||
         !(v->learned_margin >= 0.f && v->learned_margin < 10.f) || v->small_sort < 0 || v->small_sort > 2 ||
-        v->cta_stage < 0 || v->cta_stage > 1 || v->cta_narrow < 0 || v->cta_narrow > 1)
+        v->cta_stage < 0 || v->cta_stage > 1 || v->cta_narrow < 0 || v->cta_narrow > 1 || v->mid_sort < 0 ||
+        v->mid_sort > 1)
         return GALP_EINVAL;
     if (v->hub_part_shift < -16 || v->hub_part_shift > kMaxHubShift) return GALP_EINVAL;
     if (v->hub_part_shift != ctx->eng.sched.hub_shift) {

@@ -241,7 +241,7 @@ struct Engine {
     // resident blocks per SM of the mid-vertex counting and the resolve kernels (occupancy
     // API): their grid-stride loops run as one full wave, since a partial second wave
     // would start its blocks' whole shares late
-    int occ_mid = 0, occ_resolve = 0, occ_resolve_mid = 0;
+    int occ_mid = 0, occ_mid_sort = 0, occ_resolve = 0, occ_resolve_mid = 0;
     int occ_cta64 = 0, occ_cta128 = 0, occ_cta256 = 0;  // resident CTA-kernel blocks per SM
     int launch_limits();
     // hub partitions at 2^shift times the default count: plan, upload, size the pair area

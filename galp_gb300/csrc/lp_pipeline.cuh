@@ -861,6 +861,153 @@ __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
     flush_changes(changes, p.ctl);
 }
 
+// One warp per mid vertex (33..256 neighbours), counted the segmented sort + reduce way
+// (the reference's method 0, dpp/segmented_sort.cuh and the boundary/scan/reduce steps of
+// dpp/kernel.cuh, within one warp): the vertex's labels are sorted by a 256-key bitonic
+// network (8 keys per lane; sorted position i lives in lane i / 8, register i % 8; unused
+// keys are 0xFFFFFFFF and sort last), run heads are the positions whose label differs from
+// the previous one, and a run's count is the distance to the next head.  The summary and
+// the spill (runs in label order, which the unsorted-spill queries accept) are the ones
+// the hash kernels produce.  Variant `mid_sort` 1; no table, no shared memory but the tied
+// buffer.
+__device__ __forceinline__ void warp_bitonic256(uint32_t (&a)[8], int lane)
+{
+#pragma unroll
+    for (int k = 2; k <= 256; k <<= 1) {
+#pragma unroll
+        for (int jj = k >> 1; jj > 0; jj >>= 1) {
+            if (jj >= 8) {  // partner in lane ^ (jj / 8), same register
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int i = lane * 8 + j;
+                    const uint32_t o = __shfl_xor_sync(kFull, a[j], jj >> 3);
+                    const bool up = (i & k) == 0, lower = (i & jj) == 0;
+                    a[j] = (lower == up) ? min(a[j], o) : max(a[j], o);
+                }
+            } else {  // partner in this lane's registers
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const int pj = j ^ jj;
+                    if (pj > j) {
+                        const bool up = ((lane * 8 + j) & k) == 0;
+                        const uint32_t x = a[j], y = a[pj];
+                        a[j] = up ? min(x, y) : max(x, y);
+                        a[pj] = up ? max(x, y) : min(x, y);
+                    }
+                }
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(32 * kMidWarps) count_mid_sort_kernel(PipeArgs p)
+{
+    __shared__ int32_t tbuf[kMidWarps][kWarpBuf];
+    if (!ctl_active(p.ctl)) return;
+    const bool fr = frontier_on(p);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kMidWarps + w;
+    const int nw = gridDim.x * kMidWarps;
+    unsigned long long changes = 0;
+    WarpBuf tb{tbuf[w]};
+    const int nwarp_v = p.disp->pos1;  // the degree-sorted mid list's prefix of warp vertices
+    for (int i = gw; i < nwarp_v; i += nw) {
+        const int v = p.mid_v[i];
+        if (fr && !p.dirty[v]) {
+            tb.append(lane == 0 && carry_clean(p, v), v, p.tied_mid, &p.ctl->tied_mid);
+            continue;
+        }
+        const int64_t o0 = __ldg(&p.off[v]);
+        const int deg = (int)(__ldg(&p.off[v + 1]) - o0);  // 33..256
+        uint32_t a[8];
+        {
+            int nb[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int e = j * 32 + lane;  // coalesced loads; placement does not matter to the sort
+                nb[j] = e < deg ? ld_nbr(&p.nbr[o0 + e - p.nbr_shift]) : -1;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) a[j] = nb[j] >= 0 ? (uint32_t)ld_label(&p.lab_in[nb[j]]) : 0xFFFFFFFFu;
+        }
+        warp_bitonic256(a, lane);
+        // run heads: position i is valid when i < deg and a head when its label differs
+        // from position i - 1's (the previous lane's last key for register 0)
+        const uint32_t prev_last = __shfl_up_sync(kFull, a[7], 1);
+        unsigned hm = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int pos = lane * 8 + j;
+            const uint32_t prev = j ? a[j - 1] : prev_last;
+            if (pos < deg && (pos == 0 || a[j] != prev)) hm |= 1u << j;
+        }
+        // the first head at or after the next lane (suffix minimum over lanes), else deg
+        int first = hm ? lane * 8 + __ffs(hm) - 1 : deg;
+        int after = deg;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int o = __shfl_down_sync(kFull, first, off);
+            if (lane + off < 32) first = min(first, o);
+        }
+        after = __shfl_down_sync(kFull, first, 1);  // minimum over lanes > this one
+        if (lane == 31) after = deg;
+        // heads before this lane, for the runs' ranks
+        const int nh = __popc(hm);
+        int before = nh;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const int o = __shfl_up_sync(kFull, before, off);
+            if (lane >= off) before += o;
+        }
+        before -= nh;
+        // this lane's runs: count = next head position - head position
+        Sum5 part = sum5_empty();
+        int cnt[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            cnt[j] = 0;
+            if (hm & (1u << j)) {
+                const unsigned later = hm & ~((2u << j) - 1u);
+                const int next = later ? lane * 8 + __ffs(later) - 1 : after;
+                cnt[j] = next - (lane * 8 + j);
+                part.d += 1;
+                sum5_observe(part, (int)a[j], cnt[j]);
+            }
+        }
+        const Sum5 sm = sum5_warp(part);
+        // ranks of the smallest and largest candidate: heads before them (labels ascend)
+        int rmin = 0, rmax = sm.d - 1;
+        if (sm.k > 1) {
+            int lo = 0, hi = 0;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (hm & (1u << j)) {
+                    lo += (int)a[j] < sm.mn;
+                    hi += (int)a[j] < sm.mx;
+                }
+            rmin = __reduce_add_sync(kFull, lo);
+            rmax = __reduce_add_sync(kFull, hi);
+            if (sm.k > 2) {  // spill the runs in label order
+                int32_t *rl = p.run_lab + (o0 - p.nbr_shift);
+                uint16_t *rc = p.run_cnt + (o0 - p.nbr_shift);
+                int r = before;
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    if (hm & (1u << j)) {
+                        rl[r] = (int32_t)a[j];
+                        rc[r] = (uint16_t)cnt[j];
+                        ++r;
+                    }
+            }
+        }
+        const bool tied = lane == 0 && finish_counted(p, v, sm, rmin, rmax, changes);
+        tb.append(tied, v, p.tied_mid, &p.ctl->tied_mid);
+        __syncwarp();
+    }
+    tb.flush(p.tied_mid, &p.ctl->tied_mid);
+    flush_changes(changes, p.ctl);
+}
+
 // Block-wide Sum5 / pair reductions with one barrier each: warps publish partials, then
 // every warp folds all of them.  Buffers hold one entry per warp (W = THREADS / 32): buf
 // is [5][W], buf2 [2][W].  The kernel's end-of-vertex barrier orders a buffer's reads

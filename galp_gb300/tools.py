@@ -27,7 +27,7 @@ class KernelTimes(ctypes.Structure):
 class Variant(ctypes.Structure):
     _fields_ = [("agg_mode", ctypes.c_int32), ("frontier_frac", ctypes.c_float), ("learned_margin", ctypes.c_float),
                 ("small_sort", ctypes.c_int32), ("hub_part_shift", ctypes.c_int32),
-                ("cta_stage", ctypes.c_int32), ("cta_narrow", ctypes.c_int32), ("pad", ctypes.c_int32)]
+                ("cta_stage", ctypes.c_int32), ("cta_narrow", ctypes.c_int32), ("mid_sort", ctypes.c_int32)]
 
 
 class KernelStat(ctypes.Structure):

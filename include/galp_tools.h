@@ -74,7 +74,10 @@ typedef struct {
     int32_t cta_narrow;     /* 1 = vertices of 257..512 neighbours counted by 64-thread CTAs with 8 KB
                                tables, split off the 128-thread CTA range (default); 0 = all of that
                                range in 128-thread CTAs */
-    int32_t pad;
+    int32_t mid_sort;       /* vertices of 33..256 neighbours (the warp range): 1 = the segmented
+                               sort + reduce way (a 256-key bitonic sort per warp, runs from the
+                               sorted keys: the reference's method-0 counting), 0 = hash tables
+                               (default) */
 } galp_variant;
 
 /* One row of the in-core variant table (every row computes the same labels). */

@@ -195,3 +195,34 @@ def test_small_counting_variants_out_of_core_and_isolated(small_sort):
             p.run(10)
             assert p.iters_run == it and list(p.updates) == list(counts)
             assert np.array_equal(p.get_labels(), want)
+
+
+@pytest.mark.parametrize("mid_sort", [0, 1])
+def test_sort_reduce_mid_counting_variant(mid_sort):
+    # vertices of 33..256 neighbours counted by hash tables or by a warp bitonic sort and
+    # run detection (the method-0 way): the same labels and change counts, dense and with
+    # the frontier, in-core and out of core, with every warp/CTA split of the variant rows
+    for g in (galp_gb300.generate_rmat(16, 16, seed=6), galp_gb300.generate_lfr(20000, seed=8),
+              galp_gb300.generate_sbm([128] * 32, 40.0, 8.0, seed=2)):
+        assert ((g.degrees() > 32) & (g.degrees() <= 256)).sum() > 500
+        it, want, counts = oracle.run(g.offsets, g.neighbors, 10)
+        for fr in (0, 1):
+            with galp_gb300.Propagator(g, frontier=fr) as p:
+                tools.set_variant(p, mid_sort=mid_sort)
+                p.run(10)
+                assert p.iters_run == it and list(p.updates) == list(counts)
+                assert np.array_equal(p.get_labels(), want)
+    g = galp_gb300.generate_rmat(15, 16, seed=11)
+    for row in (0, 2, 4, 6):
+        with galp_gb300.Propagator(g, frontier=1) as p:
+            tools.dispatch_set(p, 2, row)
+            tools.set_variant(p, mid_sort=mid_sort)
+            p.run(8)
+            it, want, counts = oracle.run(g.offsets, g.neighbors, 8)
+            assert p.iters_run == it and np.array_equal(p.get_labels(), want)
+    it, want, counts = oracle.run(g.offsets, g.neighbors, 5, policy=2, buffer_pow=14)
+    with galp_gb300.Propagator(g, policy=2, buffer_pow=14) as p:
+        tools.set_variant(p, mid_sort=mid_sort)
+        p.run(5)
+        assert p.iters_run == it and list(p.updates) == list(counts)
+        assert np.array_equal(p.get_labels(), want)
