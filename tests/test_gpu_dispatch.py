@@ -113,9 +113,10 @@ def test_variant_defaults_and_validation():
     g = galp_gb300.generate_sbm([64] * 8, 8.0, 1.0, seed=1)
     with galp_gb300.Propagator(g) as p:
         v = tools.set_variant(p)
-        assert (v.small_sort, v.cta_narrow, v.cta_stage, v.agg_mode, v.hub_part_shift) == (2, 1, 0, 0, 1)
+        assert (v.small_sort, v.cta_narrow, v.cta_stage, v.agg_mode, v.hub_part_shift, v.mid_sort) == \
+            (2, 1, 0, 0, 1, 0)
         for bad in ({"small_sort": 3}, {"small_sort": -1}, {"cta_narrow": 2}, {"cta_stage": 2},
-                    {"agg_mode": 3}, {"frontier_frac": 1.5}, {"hub_part_shift": 99}):
+                    {"agg_mode": 3}, {"frontier_frac": 1.5}, {"hub_part_shift": 99}, {"mid_sort": 2}):
             with pytest.raises(RuntimeError):
                 tools.set_variant(p, **bad)
         assert tools.set_variant(p).small_sort == 2
