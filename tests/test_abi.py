@@ -74,3 +74,36 @@ def test_device_closed_form_matches_oracle():
         want = oracle.cf_winner(w, a, b, N) - a
         got = L.galp_debug_resolve_rank(a, d, N, int(b == N), cand.ctypes.data, k)
         assert got == want, (a, d, N, k)
+
+
+def test_ctypes_mirrors_match_the_c_structs(tmp_path):
+    """Every ctypes mirror of an include/*.h struct has the C struct's size and field
+    offsets (a plain C compiler lays the headers out; no GPU needed)."""
+    import shutil
+    import subprocess
+
+    from galp_gb300 import tools
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"galp_csr": galp_gb300._Csr, "galp_opts": galp_gb300.Opts, "galp_stats": galp_gb300.Stats,
+               "galp_sched_info": tools.SchedInfo, "galp_kernel_times": tools.KernelTimes,
+               "galp_kernel_stat": tools.KernelStat, "galp_variant": tools.Variant,
+               "galp_dispatch_row": tools.DispatchRow, "galp_tune_result": tools.TuneResult}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "galp_tools.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f in cls._fields_:
+            lines.append(f'printf("{cname} {f[0]} %zu\\n", offsetof({cname}, {f[0]}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for cname, cls in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for f in cls._fields_:
+            assert got[(cname, f[0])] == getattr(cls, f[0]).offset, (cname, f[0])
