@@ -767,7 +767,8 @@ __device__ __forceinline__ CtaHead cta_head(const PipeArgs &p, int first, int i,
 // One warp per mid vertex (33..256 neighbours): a 512-slot table of generation-tagged
 // 64-bit slots per warp (as the CTA tables: never cleared between vertices), probed over
 // up to 4 slots per neighbour.  Against 32-bit key and count arrays cleared per vertex:
-// no clear pass and one shared-memory atomic per insert.
+// no clear pass and one shared-memory atomic per insert.  The next vertex's head and its
+// neighbour IDs load while the current one is counted (as in the CTA kernels).
 __global__ void __launch_bounds__(32 * kMidWarps) count_mid64_kernel(PipeArgs p)
 {
     __shared__ unsigned long long stab[kMidWarps][kMidSCap];
@@ -1095,10 +1096,10 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t pari
 // One CTA of THREADS threads per vertex of degree <= SLOTS/2 (table of SLOTS 64-bit
 // slots in dynamic shared memory), for a range of the degree-sorted mid list.
 //
-// Software pipelining across the CTA's vertices: the next vertex's head (CtaHead) and,
-// unless staged, its first PER * THREADS neighbour IDs are loaded into registers while
-// the current vertex's labels are gathered and counted, so a vertex starts with its
-// label gathers instead of three dependent global round trips.
+// Software pipelining across the CTA's vertices: the next vertex's head (CtaHead) and, in
+// CTAs of up to 256 threads that do not stage, its first PER * THREADS neighbour IDs are
+// loaded into registers while the current vertex's labels are gathered and counted, so a
+// vertex starts with its label gathers instead of three dependent global round trips.
 //
 // STAGE: the next vertex's neighbour IDs are copied into a shared-memory stage by one
 // bulk copy (cp.async.bulk, completion on an mbarrier) while the current vertex is
